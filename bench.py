@@ -1,0 +1,359 @@
+"""Benchmark: 30-qubit ComplexDP gate layer (Haar-random U on every qubit + CZ brick), GB/s.
+
+One step = one layer on a 2^30-amplitude ComplexDP register (16 GiB, far larger than L2):
+30 Haar-random 2x2 gates (QR of a seeded complex Gaussian, phase-fixed), CZ on the 15 even
+pairs, then the 14 odd pairs. The metric is the layer's algorithmic bytes -- 2*N*16 per
+1-qubit gate and N*16 per controlled gate, the reference's own accounting
+(src/highperfkernels.cpp:370, :478) -- divided by the layer time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--qubits 30] [--math emulated|native]
+
+--impl reference times the reference's CPU implementation of the same layer on the host
+cores (the reference library built from its sources when present, else the C restatement
+in oracle/), on a 28-qubit sample of the workload. Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+for _p in (REPO, REPO / "intel-qs_gb300", REPO / "tests"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+METRIC = "30q gate-layer HBM GB/s (ComplexDP, algorithmic bytes)"
+UNIT = "GB/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def layer_bytes(n: int, amp_bytes: int = 16) -> int:
+    N = 1 << n
+    num_cz = (n // 2) + ((n - 1) // 2)
+    return n * 2 * N * amp_bytes + num_cz * N * amp_bytes
+
+
+def haar_layers(n: int, count: int, seed: int) -> list:
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        mats = []
+        for _q in range(n):
+            z = (rng.standard_normal((2, 2)) + 1j * rng.standard_normal((2, 2))) / np.sqrt(2.0)
+            q, r = np.linalg.qr(z)
+            d = np.diag(r)
+            mats.append(np.ascontiguousarray(q * (d / np.abs(d))))
+        out.append(mats)
+    return out
+
+
+def apply_layer(reg, mats, n: int, on_1q=None) -> None:
+    """Public-API layer: Apply1QubitGate on every qubit, then the CZ bricks."""
+    for q in range(n):
+        if on_1q is not None:
+            on_1q(0)
+        reg.Apply1QubitGate(q, mats[q])
+        if on_1q is not None:
+            on_1q(1)
+    for j in range(n // 2):
+        reg.ApplyCPauliZ(2 * j, 2 * j + 1)
+    for j in range((n - 1) // 2):
+        reg.ApplyCPauliZ(2 * j + 1, 2 * j + 2)
+
+
+def peak_hbm() -> tuple[float, str]:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = REPO / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "0x1", "1"):
+                    reasons.add(nm)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_layer_gbs(n: int, layers: int, seed: int, threads: int | None = None, use_ref: bool = False) -> dict:
+    """The same layer on the host cores: the reference library (when built here) or the
+    C restatement (oracle/) with all OpenMP threads."""
+    import oracle
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        oracle.set_threads(threads)
+    kind = "reference" if (use_ref and oracle.ref_available()) else "port"
+    reg = (oracle.RefRegister if kind == "reference" else oracle.OracleRegister)(n, "base", 0)
+    mats = haar_layers(n, layers, seed)
+    t0 = time.perf_counter()
+    for l in range(layers):
+        apply_layer(reg, mats[l], n)
+    dt = time.perf_counter() - t0
+    return {"kind": kind, "seconds": dt, "gbs": layers * layer_bytes(n) / dt / 1e9,
+            "cores": threads or oracle.get_threads()}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n = args.cpu_qubits
+    import oracle
+    oracle.build(ref=None)
+    threads = os.cpu_count() or 1
+    times, kind = [], None
+    for s in range(args.warmup + args.steps):
+        r = cpu_layer_gbs(n, 1, seed=100 + s, threads=threads, use_ref=True)
+        kind = r["kind"]
+        if s >= args.warmup:
+            times.append(r["seconds"])
+    t = statistics.median(times)
+    value = layer_bytes(n) / t / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Haar-random gates)",
+            "config": {"workload": f"gate layer: Haar U on each of {n} qubits + CZ brick, ComplexDP",
+                       "qubits": n, "sample": f"one {n}-qubit layer per step (the 30q layer shape at {n} qubits)"},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"one {n}-qubit layer per step, {threads} OpenMP threads"},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    import iqs_gb300 as iqs
+
+    n = args.qubits
+    stream = torch.cuda.current_stream()
+    reg = iqs.QubitRegister(n, "base", 0, math=args.math, stream=stream.cuda_stream)
+    for q in range(n):  # a dense state: every amplitude nonzero
+        reg.ApplyHadamard(q)
+    total = args.warmup + args.steps
+    mats = haar_layers(n, total, seed=1000 + rank)
+
+    # Warm-up (untimed).
+    for s in range(args.warmup):
+        apply_layer(reg, mats[s], n)
+    barrier()
+
+    # Timed region: K layers; event pairs around each 1-qubit gate launch (the dominant
+    # kernel) on the same stream.
+    kev = []
+
+    def mark(which):
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(stream)
+        if which == 0:
+            kev.append([e, None])
+        else:
+            kev[-1][1] = e
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for s in range(args.warmup, total):
+        apply_layer(reg, mats[s], n, on_1q=mark)
+    end.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = start.elapsed_time(end)
+    k_ms = [a.elapsed_time(b) for a, b in kev]
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * layer_bytes(n) / (ms_per_step * 1e-3) / 1e9
+
+    # Dominant kernel: the 1-qubit gate, algorithmic bytes 2*N*16 per launch.
+    k_avg = statistics.mean(k_ms)
+    peak, peak_src = peak_hbm()
+    achieved = 2 * (1 << n) * 16 / (k_avg * 1e-3) / 1e9
+
+    # End to end through the public API with host buffers: upload the state from pinned
+    # host memory, apply the layer, download the state, every step.
+    e2e_steps = max(1, min(args.steps, 3))
+    host = torch.empty(1 << n, dtype=torch.complex128, pin_memory=True)
+    host.copy_(torch.from_numpy(reg.GetStateVector()))
+    hbuf = host.numpy()
+    barrier()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        reg.SetStateVector(hbuf)                      # host (pinned) -> HBM
+        apply_layer(reg, mats[args.warmup + s % args.steps], n)
+        reg.GetStateVector(out=hbuf)                  # HBM -> host (pinned)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = world * layer_bytes(n) / e2e_s / 1e9
+
+    # Same layer with native FP64 arithmetic, for comparison (2 steps).
+    other = {}
+    if n >= 20 and args.compare_native and args.math == "emulated":
+        reg.SetMath("native")
+        barrier()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for s in range(2):
+            apply_layer(reg, mats[args.warmup + s % args.steps], n)
+        b.record(stream)
+        barrier()
+        nat_ms = a.elapsed_time(b) / 2
+        other = {"native_fp64": {"value": round(layer_bytes(n) / (nat_ms * 1e-3) / 1e9, 1), "ms_per_step": round(nat_ms, 3)}}
+        reg.SetMath(args.math)
+
+    del reg
+    torch.cuda.synchronize()
+
+    # Parity of the timed arithmetic on the same layer shape at 20 qubits vs the oracle.
+    parity = None
+    cpu = None
+    if rank == 0:
+        import oracle
+        oracle.build(ref=False)
+        m20 = haar_layers(20, 2, seed=7)
+        g = iqs.QubitRegister(20, "base", 0, math=args.math)
+        o = oracle.OracleRegister(20, "base", 0)
+        for r_ in (g, o):
+            for q in range(20):
+                r_.ApplyHadamard(q)
+            for l in range(2):
+                apply_layer(r_, m20[l], 20)
+        parity = float(np.max(np.abs(g.GetStateVector() - o.GetStateVector())))
+        del g
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            cpu = cpu_layer_gbs(args.cpu_qubits, 1, seed=5, threads=threads)
+
+    if rank == 0:
+        dtype = "c128: f64 storage, double-float (fp32x2) products and sums" if args.math == "emulated" else "f64"
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic (seeded Haar-random gates on a dense state)",
+            "config": {"workload": f"gate layer: Haar U on each of {n} qubits + CZ brick (15 even + 14 odd), ComplexDP",
+                       "qubits": n, "state_bytes": (1 << n) * 16, "bytes_per_step": layer_bytes(n),
+                       "math": args.math, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "state (16 GiB) far larger than L2 (129 MB); no flush needed"},
+            "roofline": {"bound": "hbm", "kernel": "1-qubit gate (k_1q_df)" if args.math == "emulated" else "1-qubit gate (k_1q)",
+                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                         "bytes_per_launch": 2 * (1 << n) * 16, "avg_launch_ms": round(k_avg, 4),
+                         "traffic": args.traffic},
+            "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": (1 << n) * 16,
+                    "d2h_bytes_per_step": (1 << n) * 16, "steps": e2e_steps,
+                    "path": "QubitRegister.SetStateVector (pinned host) + layer via public API + iqsg_download (pinned host)"},
+            "gpu_launches": args.steps * (n + (n // 2) + ((n - 1) // 2)),
+            "clocks": clk,
+            "parity": {"max_abs_err_vs_oracle": parity, "case": "same layer shape at 20 qubits, 2 layers"},
+        }
+        line.update(other)
+        if cpu is not None:
+            line["cpu_baseline"] = {"value": round(cpu["gbs"], 3), "unit": UNIT, "cores": cpu["cores"],
+                                    "kind": cpu["kind"],
+                                    "sample": f"one {args.cpu_qubits}-qubit layer (same layer shape), "
+                                              f"{cpu['seconds']:.1f} s"}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--cpu-qubits", type=int, default=28)
+    ap.add_argument("--math", choices=["emulated", "native"], default="emulated")
+    ap.add_argument("--compare-native", action="store_true", default=True)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="dram bytes per 1-qubit-gate launch from an ncu capture, if known")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

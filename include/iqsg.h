@@ -1,0 +1,209 @@
+/* iqsg.h -- C ABI of the GB300 state-vector engine (libiqsg.so).
+ *
+ * This is the drop-in boundary for the gate-application hot path of intel/intel-qs.
+ * The reference has no C ABI: its boundary is the C++ class template
+ * iqs::QubitRegister<Type> (include/qureg.hpp:127-417). Each entry point below replaces
+ * the local (single-rank) branch of one QubitRegister method, cited per function; the
+ * C++ header include/iqs_gb300/qureg.hpp and the Python package iqs_gb300 rebuild the
+ * QubitRegister API on top of these calls.
+ *
+ * Conventions
+ *  - A register of n qubits holds 2^n complex amplitudes in device memory (HBM),
+ *    interleaved (re, im) exactly like std::complex<double> (IQSG_COMPLEX_DP, 16 B)
+ *    or std::complex<float> (IQSG_COMPLEX_SP, 8 B), 256-byte aligned.
+ *  - Every qubit argument is a data POSITION: bit k of an amplitude's index is
+ *    position k. The program-qubit -> position map (iqs::Permutation,
+ *    include/permutation.hpp) is kept by the caller, as QubitRegister does.
+ *  - Gate matrices are row-major, interleaved, always double precision:
+ *    m[2*(r*dim+c)] = Re m_rc, m[2*(r*dim+c)+1] = Im m_rc (TinyMatrix layout,
+ *    include/tinymatrix.hpp). An SP register rounds them to float.
+ *  - Every call returns an iqsg_status. On failure iqsg_last_error() describes it.
+ *    Invalid arguments are rejected before any device work (the reference asserts).
+ *  - Work is queued on the register's CUDA stream. Gate calls return without waiting;
+ *    calls that return a value (probabilities, norms, amplitudes, ...) wait for it.
+ *  - All reductions accumulate in FP64 on the device, in a fixed order (deterministic).
+ */
+#ifndef IQSG_H
+#define IQSG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  IQSG_OK = 0,
+  IQSG_EINVAL = 1,   /* invalid argument (qubit position, size, map, null pointer ...) */
+  IQSG_ENOMEM = 2,   /* device or pinned-host allocation failed */
+  IQSG_EDEVICE = 3,  /* CUDA runtime error (launch failure, no device ...) */
+  IQSG_ETIMEOUT = 4, /* a bounded device-side wait gave up */
+  IQSG_ENOTSUP = 5   /* valid request this build does not support */
+} iqsg_status;
+
+typedef enum { IQSG_COMPLEX_DP = 0, IQSG_COMPLEX_SP = 1 } iqsg_precision;
+
+/* Arithmetic used by ComplexDP gate kernels.
+ *  NATIVE: IEEE FP64 fused multiply-adds (the GB300 FP64 pipe: about 0.5 T instr/s).
+ *  EMULATED: FP64 storage, products and sums in double-float (two FP32 words, about
+ *            48-bit significand) on the FP32 pipe, rounded back to FP64 on store.
+ *  ComplexSP registers always compute in FP32. */
+typedef enum { IQSG_MATH_NATIVE = 0, IQSG_MATH_EMULATED = 1 } iqsg_math;
+
+typedef struct iqsg_state iqsg_state;
+
+/* ---- errors, version ---------------------------------------------------------------- */
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char* iqsg_last_error(void);
+/* Library version as major*10000 + minor*100 + patch. */
+int iqsg_version(void);
+
+/* ---- lifecycle ------------------------------------------------------------------------ */
+
+/* Allocate a register of num_qubits qubits on the current CUDA device and zero it.
+ * stream: a cudaStream_t to queue work on, or NULL for a stream owned by the register.
+ * Replaces QubitRegister(n, style, base, tmp) allocation: src/qureg_init.cpp:149-188. */
+int iqsg_create(unsigned num_qubits, int precision, void* stream, iqsg_state** out);
+
+/* Wrap caller-owned device memory (2^n amplitudes, 256-B aligned) without copying.
+ * destroy() does not free it. Replaces the imported-state constructor
+ * QubitRegister(n, Type* state, tmp): src/qureg_init.cpp:193-200. */
+int iqsg_create_from_device(unsigned num_qubits, int precision, void* device_amps, void* stream,
+                            iqsg_state** out);
+
+/* Deep copy (device to device) into a new register on the same stream.
+ * Replaces the copy constructor: src/qureg_init.cpp:364-379. */
+int iqsg_clone(const iqsg_state* src, iqsg_state** out);
+
+/* Free the register (and its device memory unless wrapped). Replaces ~QubitRegister:
+ * src/qureg_init.cpp:452-461. Accepts NULL. */
+int iqsg_destroy(iqsg_state* h);
+
+/* Query size, precision and the device address of amplitude 0. */
+int iqsg_info(const iqsg_state* h, unsigned* num_qubits, int* precision, void** device_amps);
+
+/* Select the ComplexDP gate arithmetic (iqsg_math). Default: IQSG_MATH_NATIVE. */
+int iqsg_set_math(iqsg_state* h, int math);
+
+/* Wait for all work queued on the register's stream. */
+int iqsg_synchronize(iqsg_state* h);
+
+/* ---- initialisation and amplitude access ------------------------------------------------ */
+
+/* Set every amplitude to (re, im). Replaces InitializationWithSameAmplitudeEverywhere:
+ * src/qureg_utils.cpp:173-184 (and the "++++" style of Initialize, :342-346). */
+int iqsg_fill(iqsg_state* h, double re, double im);
+
+/* Zero the register and set amplitude data_index to 1: Initialize("base", i) with the
+ * index already mapped to data order, src/qureg_init.cpp:242-249 and :335-340. */
+int iqsg_init_basis(iqsg_state* h, uint64_t data_index);
+
+/* Write / read one amplitude at a data index. Replace SetGlobalAmplitude /
+ * GetGlobalAmplitude after program2data_ (src/qureg_utils.cpp:78-121). */
+int iqsg_set_amplitude(iqsg_state* h, uint64_t data_index, double re, double im);
+int iqsg_get_amplitude(iqsg_state* h, uint64_t data_index, double* re_im);
+
+/* Copy count amplitudes between host memory (in the register's own precision,
+ * interleaved) and the register, starting at amplitude offset. Synchronous.
+ * The reference exposes its host array directly (RawState(), operator[]:
+ * include/qureg.hpp:150-166); this is the explicit host <-> HBM transfer. */
+int iqsg_upload(iqsg_state* h, const void* host, uint64_t offset, uint64_t count);
+int iqsg_download(iqsg_state* h, void* host, uint64_t offset, uint64_t count);
+
+/* Device-to-device copy of all amplitudes (same size and precision). */
+int iqsg_copy(iqsg_state* dst, const iqsg_state* src);
+
+/* ---- gates -------------------------------------------------------------------------- */
+
+/* 2x2 gate on position pos: pairs (i, i + 2^pos) with bit pos of i clear,
+ * a0' = m00 a0 + m01 a1, a1' = m10 a0 + m11 a1.
+ * Replaces Apply1QubitGate_helper -> Loop_DN: src/qureg_apply1qubitgate.cpp:173-230,
+ * src/highperfkernels.cpp:287-380. */
+int iqsg_apply_1q(iqsg_state* h, unsigned pos, const double* m);
+
+/* 2x2 gate on tpos applied where bit cpos is 1. Replaces
+ * ApplyControlled1QubitGate_helper -> Loop_TN: src/qureg_applyctrl1qubitgate.cpp:228-406,
+ * src/highperfkernels.cpp:397-486. */
+int iqsg_apply_controlled_1q(iqsg_state* h, unsigned cpos, unsigned tpos, const double* m);
+
+/* 2x2 gate on tpos applied where all num_ctrl control positions are 1 (num_ctrl <= 8).
+ * With num_ctrl = 2 and m = X this is the Toffoli gate in one pass; the reference
+ * composes it from five controlled gates (src/qureg_applytoffoli.cpp:24-47). */
+int iqsg_apply_multi_controlled_1q(iqsg_state* h, unsigned num_ctrl, const unsigned* cpos,
+                                   unsigned tpos, const double* m);
+
+/* Dense 4x4 gate; row/column index = 2*b(pos_high) + b(pos_low).
+ * Replaces Apply2QubitGate: src/qureg_apply2qubitgate.cpp:14-73. */
+int iqsg_apply_2q(iqsg_state* h, unsigned pos_high, unsigned pos_low, const double* m);
+
+/* Swap-type gate: 2x2 m on the {|p_lo=1,p_hi=0>, |p_lo=0,p_hi=1>} subspace, with
+ * p_lo = min(p1, p2). Replaces ApplySwap_helper: src/qureg_applyswap.cpp:117-234. */
+int iqsg_apply_swaplike(iqsg_state* h, unsigned p1, unsigned p2, const double* m);
+
+/* Diagonal two-qubit gate: amp[i] *= d[2*b(p1) + b(p2)], d = 4 complex entries.
+ * Replaces ApplyDiag: src/qureg_applydiag.cpp:55-227. */
+int iqsg_apply_diag_2q(iqsg_state* h, unsigned p1, unsigned p2, const double* d);
+
+/* amp[i] *= exp(-i gamma Re diag[i]) with diag a register of the same size.
+ * Replaces qaoa::ImplementQaoaLayerBasedOnCostFunction: src/qaoa_features.cpp:248-264. */
+int iqsg_apply_cost_phase(iqsg_state* h, const iqsg_state* diag, double gamma);
+
+/* Zero the half of the amplitudes where bit pos != value (no renormalisation).
+ * Replaces CollapseQubit: src/qureg_measure.cpp:92-126. */
+int iqsg_collapse(iqsg_state* h, unsigned pos, int value);
+
+/* amp[i] *= (re, im). Replaces AmplitudeWiseScalarMultiplication: src/qureg_utils.cpp:189-199. */
+int iqsg_scale(iqsg_state* h, double re, double im);
+
+/* amp[i] += (re, im) * x[i]. Replaces AmplitudeWiseSum: src/qureg_utils.cpp:207-231. */
+int iqsg_axpy(iqsg_state* h, const iqsg_state* x, double re, double im);
+
+/* Reorder amplitudes from position map old_map to new_map (direct maps: program qubit
+ * -> position, n entries each): amp'[new.p2d(old.d2p(i))] = amp[i]. Index placement is
+ * bit-exact. Replaces PermuteLocalQubits: src/qureg_permute.cpp:57-105. */
+int iqsg_permute(iqsg_state* h, const unsigned* old_map, const unsigned* new_map);
+
+/* ---- reductions (FP64 accumulation; each waits for its result) ------------------------ */
+
+/* Sum of |amp|^2 over indices with bit pos = 1. Replaces GetProbability:
+ * src/qureg_measure.cpp:135-178. */
+int iqsg_probability(iqsg_state* h, unsigned pos, double* p);
+
+/* <psi|P|psi> for the Pauli string P = prod_k obs[k] on position pos[k]
+ * (obs: 1 = X, 2 = Y, 3 = Z; positions distinct), in one read-only pass, plus
+ * sum |amp|^2 in *norm2 (may be NULL). Replaces the basis-change + parity reduction of
+ * ExpectationValue: src/qureg_expectval.cpp:102-213 (the state is not modified). */
+int iqsg_expectation_pauli(iqsg_state* h, unsigned k, const unsigned* pos, const unsigned* obs,
+                           double* value, double* norm2);
+
+/* sum |amp|^2. ComputeNorm returns its square root: src/qureg_utils.cpp:236-256. */
+int iqsg_norm2(iqsg_state* h, double* out);
+
+/* <psi|h> = sum conj(psi_i) h_i, as re_im[2]. Replaces ComputeOverlap:
+ * src/qureg_utils.cpp:267-300. */
+int iqsg_overlap(iqsg_state* h, const iqsg_state* psi, double* re_im);
+
+/* max_i |h_i - (re, im) x_i|. Replaces MaxAbsDiff: src/qureg_utils.cpp:40-68. */
+int iqsg_max_abs_diff(iqsg_state* h, const iqsg_state* x, double re, double im, double* out);
+
+/* sum_i |h_i - x_i|^2. Replaces MaxL2NormDiff: src/qureg_utils.cpp:129-157. */
+int iqsg_l2_diff(iqsg_state* h, const iqsg_state* x, double* out);
+
+/* sum_i (Re diag_i)^power |psi_i|^2 for power 1 or 2. Replaces
+ * GetExpectationValueFromCostFunction / ...SquaredFromCostFunction:
+ * src/qaoa_features.cpp:273-331. */
+int iqsg_cost_expectation(iqsg_state* psi, const iqsg_state* diag, int power, double* out);
+
+/* Fill diag with the MaxCut value of every basis state: diag[i] = (cut(d2p(i)), 0) for the
+ * graph adj (n*n ints, symmetric, zero diagonal), map = direct position map (may be NULL
+ * for identity). *max_cut receives the largest cut. Replaces
+ * InitializeVectorAsMaxCutCostFunction: src/qaoa_features.cpp:73-143. */
+int iqsg_maxcut_cost(iqsg_state* diag, const int* adj, const unsigned* map, int* max_cut);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IQSG_H */

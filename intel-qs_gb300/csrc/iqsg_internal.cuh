@@ -1,0 +1,90 @@
+// Internal declarations shared by the libiqsg translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "iqsg.h"
+
+struct iqsg_state {
+  unsigned n = 0;          // number of qubits
+  int prec = IQSG_COMPLEX_DP;
+  uint64_t N = 0;          // 2^n amplitudes
+  void* amps = nullptr;    // device amplitudes (double2 or float2)
+  bool owns = false;       // amps allocated by this register
+  cudaStream_t stream = nullptr;
+  bool owns_stream = false;
+  int math = IQSG_MATH_NATIVE;
+  int device = 0;
+  double* scratch = nullptr;      // device: reduction partials + result slots
+  double* host_result = nullptr;  // pinned host: reduction results
+  void* tmp = nullptr;            // device: out-of-place permutation buffer (lazy)
+  size_t tmp_bytes = 0;
+};
+
+namespace iqsg {
+
+constexpr int kThreads = 256;
+// Reduction partials: one (or two) doubles per block of the first pass.
+constexpr int kMaxPartials = 4096;
+// scratch layout (doubles): [0, 2*kMaxPartials) partials, then 8 result slots.
+constexpr int kResultSlot = 2 * kMaxPartials;
+constexpr int kScratchDoubles = 2 * kMaxPartials + 8;
+
+// Records the error text for iqsg_last_error() and returns code.
+int fail(int code, const char* fmt, ...);
+// Maps a CUDA error to IQSG_EDEVICE (or IQSG_ENOMEM) with context; IQSG_OK on success.
+int cuda_status(cudaError_t e, const char* what);
+// Grid size for a grid-stride loop over `work` items, `per_thread` items per thread.
+unsigned grid_for(uint64_t work, int per_thread);
+int num_sms();
+
+template <typename R> struct V2;
+template <> struct V2<double> { using type = double2; };
+template <> struct V2<float> { using type = float2; };
+
+template <typename R> struct M2 { R re[4], im[4]; };    // m00 m01 m10 m11
+template <typename R> struct M4 { R re[16], im[16]; };  // row-major 4x4
+template <typename R> struct C1 { R re, im; };
+
+// Up to 9 sorted bit positions into which zeros are inserted to enumerate sub-blocks.
+struct Positions {
+  unsigned count;
+  unsigned p[10];
+};
+
+__host__ __device__ __forceinline__ uint64_t insert_zero(uint64_t x, unsigned pos) {
+  const uint64_t lo = x & ((uint64_t(1) << pos) - 1);
+  return ((x ^ lo) << 1) | lo;
+}
+
+// ---- launchers (native kernels, k_gates.cu) ----
+template <typename R> void launch_1q(iqsg_state* h, unsigned pos, const M2<R>& m);
+template <typename R> void launch_1q_diag(iqsg_state* h, unsigned pos, C1<R> d0, C1<R> d1, bool touch0);
+template <typename R> void launch_mc1q(iqsg_state* h, const Positions& zeros, uint64_t ctrl_mask, unsigned tpos, const M2<R>& m);
+template <typename R> void launch_phase_mask(iqsg_state* h, const Positions& zeros, uint64_t ones, C1<R> d);
+template <typename R> void launch_2q(iqsg_state* h, unsigned ph, unsigned pl, const M4<R>& m);
+template <typename R> void launch_swaplike(iqsg_state* h, unsigned plo, unsigned phi, const M2<R>& m);
+template <typename R> void launch_diag2(iqsg_state* h, unsigned p1, unsigned p2, const C1<R>* d);
+template <typename R> void launch_cost_phase(iqsg_state* h, const void* diag, double gamma);
+template <typename R> void launch_collapse(iqsg_state* h, unsigned pos, int value);
+template <typename R> void launch_scale(iqsg_state* h, C1<R> f);
+template <typename R> void launch_axpy(iqsg_state* h, const void* x, C1<R> f, bool unit);
+template <typename R> void launch_fill(iqsg_state* h, C1<R> v);
+template <typename R> void launch_permute(iqsg_state* h, const void* src, void* dst, const unsigned* src_bit_of_dst_bit);
+template <typename R> void launch_maxcut_cost(iqsg_state* h, const int* edges_uv, unsigned num_edges, const unsigned* prog_pos);
+
+// ---- reductions (k_reduce.cu); results land in h->scratch[kResultSlot + k] ----
+template <typename R> void reduce_probability(iqsg_state* h, unsigned pos);
+template <typename R> void reduce_pauli(iqsg_state* h, uint64_t xmask, uint64_t zmask, unsigned ny);
+template <typename R> void reduce_norm2(iqsg_state* h);
+template <typename R> void reduce_overlap(iqsg_state* h, const void* psi);
+template <typename R> void reduce_max_abs_diff(iqsg_state* h, const void* x, C1<R> f);
+template <typename R> void reduce_l2_diff(iqsg_state* h, const void* x);
+template <typename R> void reduce_cost_expectation(iqsg_state* h, const void* diag, int power);
+template <typename R> void reduce_max_real(iqsg_state* h);
+
+// ---- emulated-FP64 gate kernels (k_emul.cu) ----
+void launch_1q_emulated(iqsg_state* h, unsigned pos, const M2<double>& m);
+
+}  // namespace iqsg

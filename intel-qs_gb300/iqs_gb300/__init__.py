@@ -1,0 +1,21 @@
+"""iqs_gb300: GB300 state-vector engine behind the iqs::QubitRegister API.
+
+    import iqs_gb300 as iqs
+    psi = iqs.QubitRegister(20, "base", 0)
+    psi.ApplyHadamard(0)
+    psi.ApplyCPauliX(0, 1)
+    psi.ExpectationValueZZ(0, 1)
+
+All state lives in GPU memory; every operation runs as a CUDA kernel in libiqsg.so.
+"""
+from ._lib import IqsgError, LIB_PATH, lib
+from .permutation import GateCounter, Permutation
+from .qureg import QubitRegister
+from .qaoa import (GetExpectationValueFromCostFunction, GetExpectationValueSquaredFromCostFunction,
+                   ImplementQaoaLayerBasedOnCostFunction, InitializeVectorAsMaxCutCostFunction)
+
+__all__ = [
+    "QubitRegister", "Permutation", "GateCounter", "IqsgError", "LIB_PATH", "lib",
+    "InitializeVectorAsMaxCutCostFunction", "ImplementQaoaLayerBasedOnCostFunction",
+    "GetExpectationValueFromCostFunction", "GetExpectationValueSquaredFromCostFunction",
+]

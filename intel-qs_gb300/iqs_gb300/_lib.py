@@ -1,0 +1,114 @@
+"""ctypes binding of libiqsg.so (include/iqsg.h).
+
+The library is required: importing this module without it, or on a machine without a
+CUDA device when a register is created, raises. There is no CPU implementation behind
+this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libiqsg.so"
+
+IQSG_OK, IQSG_EINVAL, IQSG_ENOMEM, IQSG_EDEVICE, IQSG_ETIMEOUT, IQSG_ENOTSUP = range(6)
+COMPLEX_DP, COMPLEX_SP = 0, 1
+MATH_NATIVE, MATH_EMULATED = 0, 1
+
+_P = C.c_void_p
+_U = C.c_uint
+_U64 = C.c_uint64
+_D = C.c_double
+_DP = C.POINTER(C.c_double)
+_UP = C.POINTER(C.c_uint)
+_IP = C.POINTER(C.c_int)
+
+# name -> argtypes (every function returns int status unless listed in _RESTYPES)
+SIGNATURES = {
+    "iqsg_last_error": [],
+    "iqsg_version": [],
+    "iqsg_create": [_U, C.c_int, _P, C.POINTER(_P)],
+    "iqsg_create_from_device": [_U, C.c_int, _P, _P, C.POINTER(_P)],
+    "iqsg_clone": [_P, C.POINTER(_P)],
+    "iqsg_destroy": [_P],
+    "iqsg_info": [_P, _UP, C.POINTER(C.c_int), C.POINTER(_P)],
+    "iqsg_set_math": [_P, C.c_int],
+    "iqsg_synchronize": [_P],
+    "iqsg_fill": [_P, _D, _D],
+    "iqsg_init_basis": [_P, _U64],
+    "iqsg_set_amplitude": [_P, _U64, _D, _D],
+    "iqsg_get_amplitude": [_P, _U64, _DP],
+    "iqsg_upload": [_P, _P, _U64, _U64],
+    "iqsg_download": [_P, _P, _U64, _U64],
+    "iqsg_copy": [_P, _P],
+    "iqsg_apply_1q": [_P, _U, _DP],
+    "iqsg_apply_controlled_1q": [_P, _U, _U, _DP],
+    "iqsg_apply_multi_controlled_1q": [_P, _U, _UP, _U, _DP],
+    "iqsg_apply_2q": [_P, _U, _U, _DP],
+    "iqsg_apply_swaplike": [_P, _U, _U, _DP],
+    "iqsg_apply_diag_2q": [_P, _U, _U, _DP],
+    "iqsg_apply_cost_phase": [_P, _P, _D],
+    "iqsg_collapse": [_P, _U, C.c_int],
+    "iqsg_scale": [_P, _D, _D],
+    "iqsg_axpy": [_P, _P, _D, _D],
+    "iqsg_permute": [_P, _UP, _UP],
+    "iqsg_probability": [_P, _U, _DP],
+    "iqsg_expectation_pauli": [_P, _U, _UP, _UP, _DP, _DP],
+    "iqsg_norm2": [_P, _DP],
+    "iqsg_overlap": [_P, _P, _DP],
+    "iqsg_max_abs_diff": [_P, _P, _D, _D, _DP],
+    "iqsg_l2_diff": [_P, _P, _DP],
+    "iqsg_cost_expectation": [_P, _P, C.c_int, _DP],
+    "iqsg_maxcut_cost": [_P, _IP, _UP, _IP],
+}
+_RESTYPES = {"iqsg_last_error": C.c_char_p}
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"libiqsg.so not found at {LIB_PATH}; build it first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, argtypes in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argtypes
+        fn.restype = _RESTYPES.get(name, C.c_int)
+    return lib
+
+
+lib = _load()
+
+
+class IqsgError(RuntimeError):
+    """A CUDA-side failure reported by libiqsg (status IQSG_EDEVICE / IQSG_ETIMEOUT / ...)."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+
+
+def check(status: int) -> None:
+    """Raise the Python exception matching an iqsg_status (EINVAL -> ValueError,
+    ENOMEM -> MemoryError, others -> IqsgError)."""
+    if status == IQSG_OK:
+        return
+    msg = (lib.iqsg_last_error() or b"").decode(errors="replace")
+    if status == IQSG_EINVAL:
+        raise ValueError(msg)
+    if status == IQSG_ENOMEM:
+        raise MemoryError(msg)
+    raise IqsgError(status, msg)
+
+
+def dptr(a) -> "C.POINTER(C.c_double)":
+    return a.ctypes.data_as(_DP)
+
+
+def uptr(a) -> "C.POINTER(C.c_uint)":
+    return a.ctypes.data_as(_UP)
+
+
+def iptr(a) -> "C.POINTER(C.c_int)":
+    return a.ctypes.data_as(_IP)

@@ -1,0 +1,139 @@
+"""Host-side qubit order: program qubit <-> data position (include/permutation.hpp)."""
+from __future__ import annotations
+
+from typing import Iterable, List
+
+
+class Permutation:
+    """Program-qubit -> data-position map, as iqs::Permutation (include/permutation.hpp:31-408).
+
+    ``map[q]`` is the position of program qubit q, ``imap[p]`` the program qubit stored at
+    position p. Bit p of a data index is position p.
+    """
+
+    def __init__(self, m, style_of_map: str = "direct"):
+        if isinstance(m, int):
+            m = list(range(m))
+        self.map: List[int] = []
+        self.imap: List[int] = []
+        self.SetNewPermutationFromMap(list(m), style_of_map)
+
+    @property
+    def num_elements(self) -> int:
+        return len(self.map)
+
+    def __getitem__(self, q: int) -> int:
+        if not 0 <= q < len(self.map):
+            raise IndexError(f"qubit {q} out of range for {len(self.map)} qubits")
+        return self.map[q]
+
+    def __len__(self) -> int:
+        return len(self.map)
+
+    def __eq__(self, other) -> bool:
+        return isinstance(other, Permutation) and self.map == other.map
+
+    def SetNewPermutationFromMap(self, m: List[int], style_of_map: str = "direct") -> None:
+        """include/permutation.hpp:157-185; raises ValueError where the reference asserts."""
+        n = len(m)
+        if sorted(m) != list(range(n)):
+            raise ValueError(f"not a permutation of 0..{n - 1}: {m}")
+        if style_of_map == "direct":
+            self.map = list(m)
+            self.imap = [0] * n
+            for q, p in enumerate(self.map):
+                self.imap[p] = q
+        elif style_of_map == "inverse":
+            self.imap = list(m)
+            self.map = [0] * n
+            for p, q in enumerate(self.imap):
+                self.map[q] = p
+        else:
+            raise ValueError(f"style_of_map must be 'direct' or 'inverse', not {style_of_map!r}")
+
+    def ExchangeTwoElements(self, e1: int, e2: int) -> None:
+        """include/permutation.hpp:193-201."""
+        p1, p2 = self.map[e1], self.map[e2]
+        self.map[e1], self.map[e2] = p2, p1
+        self.imap[p1], self.imap[p2] = e2, e1
+
+    def Find(self, position: int) -> int:
+        return self.imap[position]
+
+    def data2program_(self, v: int) -> int:
+        """Bit q of the result = bit map[q] of v (include/permutation.hpp:249-255)."""
+        out = 0
+        for q, p in enumerate(self.map):
+            out |= ((v >> p) & 1) << q
+        return out
+
+    def program2data_(self, v: int) -> int:
+        """Bit p of the result = bit imap[p] of v (include/permutation.hpp:258-264)."""
+        out = 0
+        for p, q in enumerate(self.imap):
+            out |= ((v >> q) & 1) << p
+        return out
+
+    def GetMapStr(self) -> str:
+        return "".join(f" {p}" for p in self.map)
+
+    def GetImapStr(self) -> str:
+        return "".join(f" {q}" for q in self.imap)
+
+    def copy(self) -> "Permutation":
+        return Permutation(self.map, "direct")
+
+
+class GateCounter:
+    """One/two-qubit gate counts and greedy depth (include/gate_counter.hpp:18-95)."""
+
+    def __init__(self, num_qubits: int):
+        self.num_qubits = num_qubits
+        self.total_gate_count = 0
+        self.one_qubit_gate_count = 0
+        self.two_qubit_gate_count = 0
+        self.parallel_depth = [0] * num_qubits
+
+    def Reset(self) -> None:
+        self.parallel_depth = [0] * self.num_qubits
+
+    def GetTotalGateCount(self) -> int:
+        return self.total_gate_count
+
+    def GetOneQubitGateCount(self) -> int:
+        return self.one_qubit_gate_count
+
+    def GetTwoQubitGateCount(self) -> int:
+        return self.two_qubit_gate_count
+
+    def GetParallelDepth(self) -> int:
+        return max(self.parallel_depth) if self.parallel_depth else 0
+
+    def OneQubitIncrement(self, q: int) -> None:
+        self.total_gate_count += 1
+        self.one_qubit_gate_count += 1
+        self.parallel_depth[q] += 1
+
+    def TwoQubitIncrement(self, q0: int, q1: int) -> None:
+        self.total_gate_count += 1
+        self.two_qubit_gate_count += 1
+        d = max(self.parallel_depth[q0], self.parallel_depth[q1]) + 1
+        self.parallel_depth[q0] = d
+        self.parallel_depth[q1] = d
+
+    def Breakdown(self) -> str:
+        s = (f"The quantum circuit is composed of {self.one_qubit_gate_count} one-qubit gates and "
+             f"{self.two_qubit_gate_count} two-qubitgates, for a total of {self.total_gate_count} gates.\n"
+             f"The greedy depth (all gates lasting one clock cycle) is {self.GetParallelDepth()}.\n")
+        print(s, end="")
+        return s
+
+
+def check_distinct(qubits: Iterable[int], n: int, what: str) -> None:
+    seen = set()
+    for q in qubits:
+        if not 0 <= q < n:
+            raise ValueError(f"{what}: qubit {q} out of range for {n} qubits")
+        if q in seen:
+            raise ValueError(f"{what}: qubit {q} repeated")
+        seen.add(q)
