@@ -197,7 +197,11 @@ def run_ours(args) -> None:
     import iqs_gb300 as iqs
 
     n = args.qubits
-    stream = torch.cuda.current_stream()
+    # A dedicated (non-default) stream: the register queues every kernel on it and the
+    # CUDA events below are recorded on the same stream.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
     reg = iqs.QubitRegister(n, "base", 0, math=args.math, stream=stream.cuda_stream)
     for q in range(n):  # a dense state: every amplitude nonzero
         reg.ApplyHadamard(q)

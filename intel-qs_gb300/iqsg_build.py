@@ -1,7 +1,8 @@
 """Build libiqsg.so (the CUDA kernels + C ABI) in-tree with nvcc, for sm_103a only.
 
 Each .cu under intel-qs_gb300/csrc compiles to an object in parallel, then nvcc links the
-shared library next to this file. Objects go to intel-qs_gb300/_build (git-ignored).
+shared library into the iqs_gb300 package directory, where iqs_gb300._lib loads it.
+Objects go to intel-qs_gb300/_build (git-ignored).
 A rebuild happens only when a source or header is newer than the library.
 """
 from __future__ import annotations
@@ -12,8 +13,8 @@ import subprocess
 from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
-PKG_DIR = Path(__file__).resolve().parent
-ROOT = PKG_DIR.parent                      # intel-qs_gb300/
+ROOT = Path(__file__).resolve().parent     # intel-qs_gb300/
+PKG_DIR = ROOT / "iqs_gb300"               # the Python package that loads the library
 REPO = ROOT.parent
 CSRC = ROOT / "csrc"
 INCLUDE = REPO / "include"

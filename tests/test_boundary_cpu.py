@@ -21,7 +21,7 @@ def declared_symbols():
 
 @pytest.fixture(scope="module")
 def built_lib():
-    from iqs_gb300 import _build
+    import iqsg_build as _build
     return _build.build()
 
 
