@@ -202,6 +202,22 @@ int iqsg_cost_expectation(iqsg_state* psi, const iqsg_state* diag, int power, do
  * InitializeVectorAsMaxCutCostFunction: src/qaoa_features.cpp:73-143. */
 int iqsg_maxcut_cost(iqsg_state* diag, const int* adj, const unsigned* map, int* max_cut);
 
+/* ---- allocation-free measurement -------------------------------------------------------- */
+
+/* Probability of |1> on position pos (sum of |amp|^2 over indices with that bit set) for
+ * 2^num_qubits amplitudes at device_amps, written to *device_result (device memory),
+ * queued on stream (NULL = legacy default stream); returns without waiting.
+ * No counterpart in the reference: this is iqsg_probability for callers that cannot
+ * allocate device memory at that point (HBM already full, no implicit device-wide
+ * synchronisation allowed, or a framework that owns all device memory). It calls no
+ * cudaMalloc / cudaFree: its partial sums live in a static 16 KiB device array (2048
+ * doubles) that every GPU loading the library keeps until exit. The first call on each
+ * device looks that array up and should come before any stream capture. All calls share
+ * the array, so calls that overlap on the GPU race. Sizes it cannot serve (num_qubits > 40,
+ * or more than 2048 first-pass blocks) are rejected with IQSG_EINVAL. */
+int iqsg_probability_static(const void* device_amps, unsigned num_qubits, int precision, unsigned pos,
+                            double* device_result, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

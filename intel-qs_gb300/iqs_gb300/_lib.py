@@ -61,6 +61,7 @@ SIGNATURES = {
     "iqsg_l2_diff": [_P, _P, _DP],
     "iqsg_cost_expectation": [_P, _P, C.c_int, _DP],
     "iqsg_maxcut_cost": [_P, _IP, _UP, _IP],
+    "iqsg_probability_static": [_P, _U, C.c_int, _U, _P, _P],
 }
 _RESTYPES = {"iqsg_last_error": C.c_char_p}
 
