@@ -205,16 +205,26 @@ def run_ours(args) -> None:
     reg = iqs.QubitRegister(n, "base", 0, math=args.math, stream=stream.cuda_stream)
     for q in range(n):  # a dense state: every amplitude nonzero
         reg.ApplyHadamard(q)
+    if args.width:
+        reg.SetSweepWidth(args.width)
+    if args.fusion:
+        reg.TurnOnFusion()
     total = args.warmup + args.steps
     mats = haar_layers(n, total, seed=1000 + rank)
 
+    def step(s, on_1q=None):
+        """One layer through the public API; with fusion on, the queued gates are applied
+        in fused passes by ApplyFusedGates (the reference's own fusion entry points)."""
+        apply_layer(reg, mats[s], n, on_1q=on_1q)
+        return reg.ApplyFusedGates() if args.fusion else n + (n // 2) + ((n - 1) // 2)
+
     # Warm-up (untimed).
     for s in range(args.warmup):
-        apply_layer(reg, mats[s], n)
+        step(s)
     barrier()
 
-    # Timed region: K layers; event pairs around each 1-qubit gate launch (the dominant
-    # kernel) on the same stream.
+    # Timed region: K layers on the register's stream. Without fusion, event pairs also
+    # bracket each 1-qubit gate launch (the dominant kernel).
     kev = []
 
     def mark(which):
@@ -229,14 +239,14 @@ def run_ours(args) -> None:
     clocks.start()
     barrier()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
     start.record(stream)
     for s in range(args.warmup, total):
-        apply_layer(reg, mats[s], n, on_1q=mark)
+        launches += step(s, on_1q=None if args.fusion else mark)
     end.record(stream)
     barrier()
     clk = clocks.stop()
     ms = start.elapsed_time(end)
-    k_ms = [a.elapsed_time(b) for a, b in kev]
     if dist is not None:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -244,8 +254,16 @@ def run_ours(args) -> None:
     ms_per_step = ms / args.steps
     value = world * layer_bytes(n) / (ms_per_step * 1e-3) / 1e9
 
-    # Dominant kernel: the 1-qubit gate, algorithmic bytes 2*N*16 per launch.
-    k_avg = statistics.mean(k_ms)
+    # Dominant kernel. Fused: every launch in the timed region is a full pass over the
+    # state (2*N*16 bytes), so the average launch time is the region time / launches.
+    # Unfused: the 1-qubit gate kernel, timed by its event pairs.
+    if args.fusion:
+        k_avg = ms / launches
+        kname = ("k_sweep_df (fused pass, emulated FP64)" if args.math == "emulated"
+                 else "k_sweep_native<double> (fused pass)")
+    else:
+        k_avg = statistics.mean(a.elapsed_time(b) for a, b in kev)
+        kname = "k_1q_df (1-qubit gate, emulated FP64)" if args.math == "emulated" else "k_1q<double>"
     peak, peak_src = peak_hbm()
     achieved = 2 * (1 << n) * 16 / (k_avg * 1e-3) / 1e9
 
@@ -259,7 +277,7 @@ def run_ours(args) -> None:
     t0 = time.perf_counter()
     for s in range(e2e_steps):
         reg.SetStateVector(hbuf)                      # host (pinned) -> HBM
-        apply_layer(reg, mats[args.warmup + s % args.steps], n)
+        step(args.warmup + s % args.steps)
         reg.GetStateVector(out=hbuf)                  # HBM -> host (pinned)
     barrier()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
@@ -273,7 +291,7 @@ def run_ours(args) -> None:
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         for s in range(2):
-            apply_layer(reg, mats[args.warmup + s % args.steps], n)
+            step(args.warmup + s % args.steps)
         b.record(stream)
         barrier()
         nat_ms = a.elapsed_time(b) / 2
@@ -291,6 +309,8 @@ def run_ours(args) -> None:
         oracle.build(ref=False)
         m20 = haar_layers(20, 2, seed=7)
         g = iqs.QubitRegister(20, "base", 0, math=args.math)
+        if args.fusion:
+            g.TurnOnFusion()
         o = oracle.OracleRegister(20, "base", 0)
         for r_ in (g, o):
             for q in range(20):
@@ -312,9 +332,10 @@ def run_ours(args) -> None:
             "data": "synthetic (seeded Haar-random gates on a dense state)",
             "config": {"workload": f"gate layer: Haar U on each of {n} qubits + CZ brick (15 even + 14 odd), ComplexDP",
                        "qubits": n, "state_bytes": (1 << n) * 16, "bytes_per_step": layer_bytes(n),
-                       "math": args.math, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "math": args.math, "fusion": bool(args.fusion), "sweep_width": args.width or "default",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "state (16 GiB) far larger than L2 (129 MB); no flush needed"},
-            "roofline": {"bound": "hbm", "kernel": "1-qubit gate (k_1q_df)" if args.math == "emulated" else "1-qubit gate (k_1q)",
+            "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_src,
                          "bytes_per_launch": 2 * (1 << n) * 16, "avg_launch_ms": round(k_avg, 4),
@@ -322,7 +343,7 @@ def run_ours(args) -> None:
             "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": (1 << n) * 16,
                     "d2h_bytes_per_step": (1 << n) * 16, "steps": e2e_steps,
                     "path": "QubitRegister.SetStateVector (pinned host) + layer via public API + iqsg_download (pinned host)"},
-            "gpu_launches": args.steps * (n + (n // 2) + ((n - 1) // 2)),
+            "gpu_launches": launches,
             "clocks": clk,
             "parity": {"max_abs_err_vs_oracle": parity, "case": "same layer shape at 20 qubits, 2 layers"},
         }
@@ -347,6 +368,9 @@ def main() -> None:
     ap.add_argument("--cpu-qubits", type=int, default=28)
     ap.add_argument("--math", choices=["emulated", "native"], default="emulated")
     ap.add_argument("--compare-native", action="store_true", default=True)
+    ap.add_argument("--no-fusion", dest="fusion", action="store_false", default=True,
+                    help="apply the layer gate by gate (one kernel per gate)")
+    ap.add_argument("--width", type=int, default=0, help="fused-pass width (target qubits per pass; 0 = default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per 1-qubit-gate launch from an ncu capture, if known")

@@ -165,6 +165,42 @@ int iqsg_axpy(iqsg_state* h, const iqsg_state* x, double re, double im);
  * bit-exact. Replaces PermuteLocalQubits: src/qureg_permute.cpp:57-105. */
 int iqsg_permute(iqsg_state* h, const unsigned* old_map, const unsigned* new_map);
 
+/* ---- fused gate streams ------------------------------------------------------------------ */
+
+/* One gate of a stream for iqsg_apply_ops. Positions are data positions; matrices as above. */
+typedef enum {
+  IQSG_OP_1Q = 0,       /* 2x2 m on t0 */
+  IQSG_OP_CTRL = 1,     /* 2x2 m on t0 where all nctrl positions ctrl[] are 1 */
+  IQSG_OP_2Q = 2,       /* dense 4x4 m, row/column index 2*b(t0) + b(t1) */
+  IQSG_OP_SWAPLIKE = 3, /* 2x2 m on the {|lo=1,hi=0>, |lo=0,hi=1>} pair of positions t0, t1 */
+  IQSG_OP_DIAG2 = 4,    /* amp *= m[2*b(t0) + b(t1)] (4 complex entries) */
+  IQSG_OP_PHASE = 5     /* amp *= m[0] where (index & mask) == value */
+} iqsg_op_kind;
+
+typedef struct {
+  int32_t kind;
+  uint32_t t0, t1;
+  uint32_t nctrl;
+  uint32_t ctrl[4];
+  uint64_t mask, value;
+  double m[32];
+} iqsg_op;
+
+/* Apply count gates in order, packed into fused sweeps: each sweep loads every group of 2^K
+ * amplitudes spanned by up to K target positions once, applies all its gates in registers
+ * (diagonal gates and controls on any position ride along) and stores the group once.
+ * The result equals applying the gates one by one (bit-identical in native FP64/FP32).
+ * *sweeps (may be NULL) receives the number of state passes launched.
+ * Replaces the reference's cache-blocked replay of buffered gates, ApplyFusedGates:
+ * src/qureg_fusion.cpp:55-94. */
+int iqsg_apply_ops(iqsg_state* h, const iqsg_op* ops, unsigned count, unsigned* sweeps);
+
+/* Largest number of target positions per sweep (1..4; 0 restores the default: 4 for
+ * ComplexSP, 3 for native ComplexDP, 2 for emulated ComplexDP, which is capped at 3).
+ * The reference's counterpart is the log2llc block size of TurnOnFusion:
+ * src/qureg_fusion.cpp:12-31. */
+int iqsg_set_sweep_width(iqsg_state* h, unsigned kmax);
+
 /* ---- reductions (FP64 accumulation; each waits for its result) ------------------------ */
 
 /* Sum of |amp|^2 over indices with bit pos = 1. Replaces GetProbability:

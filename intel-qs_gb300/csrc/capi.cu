@@ -106,17 +106,40 @@ Positions sorted_positions(std::vector<unsigned> v) {
   return z;
 }
 
-// Wait for a reduction and copy k result doubles to out.
+// A kernel whose bounded wait ran out leaves a nonzero word at scratch[kErrorSlot]; the
+// next call that waits for the stream reports it (and clears it).
+int take_device_error(iqsg_state* h, unsigned long long word, const char* what) {
+  if (!word) return IQSG_OK;
+  cudaMemsetAsync(h->scratch + kErrorSlot, 0, sizeof(unsigned long long), h->stream);
+  return fail(IQSG_ETIMEOUT, "%s: a kernel gave up waiting for its data copies (device error word %llu)", what, word);
+}
+
+// Wait for a reduction and copy k result doubles to out (with the device error word).
 int fetch_results(iqsg_state* h, int k, double* out, const char* what) {
   int st = after_launch(what);
   if (st) return st;
-  st = cuda_status(cudaMemcpyAsync(h->host_result, h->scratch + kResultSlot, sizeof(double) * k,
+  st = cuda_status(cudaMemcpyAsync(h->host_result, h->scratch + kResultSlot, sizeof(double) * 9,
                                    cudaMemcpyDeviceToHost, h->stream), what);
   if (st) return st;
   st = cuda_status(cudaStreamSynchronize(h->stream), what);
   if (st) return st;
+  unsigned long long word;
+  std::memcpy(&word, h->host_result + (kErrorSlot - kResultSlot), sizeof word);
+  if ((st = take_device_error(h, word, what))) return st;
   for (int i = 0; i < k; ++i) out[i] = h->host_result[i];
   return IQSG_OK;
+}
+
+// Wait for the stream, then check the device error word.
+int sync_and_check(iqsg_state* h, const char* what) {
+  int st = cuda_status(cudaMemcpyAsync(h->host_result + 8, h->scratch + kErrorSlot, sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, h->stream), what);
+  if (st) return st;
+  st = cuda_status(cudaStreamSynchronize(h->stream), what);
+  if (st) return st;
+  unsigned long long word;
+  std::memcpy(&word, h->host_result + 8, sizeof word);
+  return take_device_error(h, word, what);
 }
 
 template <typename F>
@@ -126,10 +149,31 @@ int dispatch(const iqsg_state* h, F&& f) {
   return IQSG_OK;
 }
 
+// ComplexDP gates other than the plain 2x2 run as one-gate sweeps: exchanges (X, CNOT,
+// SWAP) and sign / +-i phases (Z, CZ, S) become exact data movement with no FP64
+// instruction, and the emulated-FP64 mode covers every gate class.
+int single_op(iqsg_state* h, const iqsg_op& op) { return iqsg_apply_ops(h, &op, 1, nullptr); }
+
+iqsg_op make_op(int kind, unsigned t0, unsigned t1, const double* m, int nm) {
+  iqsg_op op;
+  std::memset(&op, 0, sizeof op);
+  op.kind = kind;
+  op.t0 = t0;
+  op.t1 = t1;
+  for (int k = 0; k < nm; ++k) op.m[k] = m[k];
+  return op;
+}
+
 // Controlled / multi-controlled 2x2 with the diagonal shortcut: when m01 = m10 = 0 and
 // m00 = 1 only the sub-block with every control and the target set changes.
 int apply_controlled(iqsg_state* h, const std::vector<unsigned>& ctrl, unsigned tpos, const double* m,
                      const char* what) {
+  if (h->prec == IQSG_COMPLEX_DP && ctrl.size() <= 4) {
+    iqsg_op op = make_op(IQSG_OP_CTRL, tpos, 0, m, 8);
+    op.nctrl = (uint32_t)ctrl.size();
+    for (size_t k = 0; k < ctrl.size(); ++k) op.ctrl[k] = ctrl[k];
+    return single_op(h, op);
+  }
   uint64_t cmask = 0;
   std::vector<unsigned> all = ctrl;
   all.push_back(tpos);
@@ -181,8 +225,9 @@ int iqsg_create(unsigned num_qubits, int precision, void* stream, iqsg_state** o
   if (!st) st = cuda_status(cudaMalloc(&h->amps, h->N * amp_bytes(precision)), "iqsg_create: state allocation");
   if (!st) h->owns = true;
   if (!st) st = cuda_status(cudaMalloc(&h->scratch, sizeof(double) * kScratchDoubles), "iqsg_create: scratch");
-  if (!st) st = cuda_status(cudaMallocHost(&h->host_result, sizeof(double) * 8), "iqsg_create: pinned result");
+  if (!st) st = cuda_status(cudaMallocHost(&h->host_result, sizeof(double) * 16), "iqsg_create: pinned result");
   if (!st) st = cuda_status(cudaMemsetAsync(h->amps, 0, h->N * amp_bytes(precision), h->stream), "iqsg_create: zero");
+  if (!st) st = cuda_status(cudaMemsetAsync(h->scratch, 0, sizeof(double) * kScratchDoubles, h->stream), "iqsg_create: scratch");
   if (st) {
     cudaGetLastError();
     iqsg_destroy(h);
@@ -217,7 +262,8 @@ int iqsg_create_from_device(unsigned num_qubits, int precision, void* device_amp
     h->owns_stream = (st == IQSG_OK);
   }
   if (!st) st = cuda_status(cudaMalloc(&h->scratch, sizeof(double) * kScratchDoubles), "iqsg_create_from_device: scratch");
-  if (!st) st = cuda_status(cudaMallocHost(&h->host_result, sizeof(double) * 8), "iqsg_create_from_device: pinned");
+  if (!st) st = cuda_status(cudaMallocHost(&h->host_result, sizeof(double) * 16), "iqsg_create_from_device: pinned");
+  if (!st) st = cuda_status(cudaMemsetAsync(h->scratch, 0, sizeof(double) * kScratchDoubles, h->stream), "iqsg_create_from_device: scratch");
   if (st) {
     cudaGetLastError();
     iqsg_destroy(h);
@@ -280,7 +326,7 @@ int iqsg_set_math(iqsg_state* h, int math) {
 int iqsg_synchronize(iqsg_state* h) {
   int st = check_h(h);
   if (st) return st;
-  return cuda_status(cudaStreamSynchronize(h->stream), "iqsg_synchronize");
+  return sync_and_check(h, "iqsg_synchronize");
 }
 
 int iqsg_fill(iqsg_state* h, double re, double im) {
@@ -365,7 +411,7 @@ int iqsg_download(iqsg_state* h, void* host, uint64_t offset, uint64_t count) {
   st = cuda_status(cudaMemcpyAsync(host, (const char*)h->amps + offset * b, count * b, cudaMemcpyDeviceToHost,
                                    h->stream), "iqsg_download");
   if (st) return st;
-  return cuda_status(cudaStreamSynchronize(h->stream), "iqsg_download");
+  return sync_and_check(h, "iqsg_download");
 }
 
 int iqsg_copy(iqsg_state* dst, const iqsg_state* src) {
@@ -388,6 +434,8 @@ int iqsg_apply_1q(iqsg_state* h, unsigned pos, const double* m) {
   if (!m) return fail(IQSG_EINVAL, "iqsg_apply_1q: null matrix");
   if ((st = check_pos(h, pos, "iqsg_apply_1q"))) return st;
   const bool diag = m[2] == 0 && m[3] == 0 && m[4] == 0 && m[5] == 0;
+  if (h->prec == IQSG_COMPLEX_DP && (diag || (m[0] == 0 && m[1] == 0 && m[6] == 0 && m[7] == 0)))
+    return single_op(h, make_op(IQSG_OP_1Q, pos, 0, m, 8));
   if (diag) {
     const bool one0 = is_one(m[0], m[1]);
     if (one0 && is_one(m[6], m[7])) return IQSG_OK;  // identity
@@ -452,6 +500,7 @@ int iqsg_apply_2q(iqsg_state* h, unsigned pos_high, unsigned pos_low, const doub
   if ((st = check_pos(h, pos_high, "iqsg_apply_2q"))) return st;
   if ((st = check_pos(h, pos_low, "iqsg_apply_2q"))) return st;
   if (pos_high == pos_low) return fail(IQSG_EINVAL, "iqsg_apply_2q: positions coincide (%u)", pos_low);
+  if (h->prec == IQSG_COMPLEX_DP) return single_op(h, make_op(IQSG_OP_2Q, pos_high, pos_low, m, 32));
   dispatch(h, [&](auto r) {
     using R = decltype(r);
     M4<R> mm;
@@ -468,6 +517,7 @@ int iqsg_apply_swaplike(iqsg_state* h, unsigned p1, unsigned p2, const double* m
   if ((st = check_pos(h, p1, "iqsg_apply_swaplike"))) return st;
   if ((st = check_pos(h, p2, "iqsg_apply_swaplike"))) return st;
   if (p1 == p2) return fail(IQSG_EINVAL, "iqsg_apply_swaplike: positions coincide (%u)", p1);
+  if (h->prec == IQSG_COMPLEX_DP) return single_op(h, make_op(IQSG_OP_SWAPLIKE, p1, p2, m, 8));
   const unsigned lo = p1 < p2 ? p1 : p2, hi = p1 < p2 ? p2 : p1;
   dispatch(h, [&](auto r) {
     using R = decltype(r);
@@ -483,6 +533,7 @@ int iqsg_apply_diag_2q(iqsg_state* h, unsigned p1, unsigned p2, const double* d)
   if ((st = check_pos(h, p1, "iqsg_apply_diag_2q"))) return st;
   if ((st = check_pos(h, p2, "iqsg_apply_diag_2q"))) return st;
   if (p1 == p2) return fail(IQSG_EINVAL, "iqsg_apply_diag_2q: positions coincide (%u)", p1);
+  if (h->prec == IQSG_COMPLEX_DP) return single_op(h, make_op(IQSG_OP_DIAG2, p1, p2, d, 8));
   if (is_one(d[0], d[1]) && is_one(d[2], d[3]) && is_one(d[4], d[5])) {
     if (is_one(d[6], d[7])) return IQSG_OK;
     Positions z = sorted_positions({p1, p2});

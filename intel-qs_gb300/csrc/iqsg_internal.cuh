@@ -20,6 +20,8 @@ struct iqsg_state {
   double* host_result = nullptr;  // pinned host: reduction results
   void* tmp = nullptr;            // device: out-of-place permutation buffer (lazy)
   size_t tmp_bytes = 0;
+  unsigned sweep_width = 0;       // fused-sweep width limit (0 = default for the precision)
+  bool no_bulk = false;           // force the non-pipelined sweep kernels (comparison / tests)
 };
 
 namespace iqsg {
@@ -29,7 +31,11 @@ constexpr int kThreads = 256;
 constexpr int kMaxPartials = 4096;
 // scratch layout (doubles): [0, 2*kMaxPartials) partials, then 8 result slots.
 constexpr int kResultSlot = 2 * kMaxPartials;
-constexpr int kScratchDoubles = 2 * kMaxPartials + 8;
+constexpr int kScratchDoubles = 2 * kMaxPartials + 16;
+// scratch[kErrorSlot] (as unsigned long long): set by a kernel whose bounded wait ran out.
+constexpr int kErrorSlot = 2 * kMaxPartials + 8;
+// Registers from this size up use the bulk-copy pipelined sweep kernels.
+constexpr unsigned kBulkMinQubits = 16;
 
 // Records the error text for iqsg_last_error() and returns code.
 int fail(int code, const char* fmt, ...);
@@ -57,6 +63,46 @@ __host__ __device__ __forceinline__ uint64_t insert_zero(uint64_t x, unsigned po
   const uint64_t lo = x & ((uint64_t(1) << pos) - 1);
   return ((x ^ lo) << 1) | lo;
 }
+
+#if defined(__CUDACC__)
+// (m0r + i m0i) a + (m1r + i m1i) b with an explicit FMA order, shared by the per-gate and
+// the fused kernels so both produce bit-identical results.
+template <typename R>
+__device__ __forceinline__ void row2_fma(R m0r, R m0i, R m1r, R m1i, R ar, R ai, R br, R bi, R& orr, R& oi) {
+  R t = m1i * bi;
+  t = fma(m1r, br, -t);
+  t = fma(-m0i, ai, t);
+  orr = fma(m0r, ar, t);
+  R u = m1i * br;
+  u = fma(m1r, bi, u);
+  u = fma(m0i, ar, u);
+  oi = fma(m0r, ai, u);
+}
+
+// (fr + i fi) a, explicit FMA order (shared like row2_fma).
+template <typename R>
+__device__ __forceinline__ void cmul_fma(R fr, R fi, R ar, R ai, R& orr, R& oi) {
+  orr = fma(fr, ar, -(fi * ai));
+  oi = fma(fr, ai, fi * ar);
+}
+
+// Row of a 4x4 times (v0..v3): sum_c (mr_c + i mi_c) v_c, explicit FMA order.
+template <typename R>
+__device__ __forceinline__ void row4_fma(const R* mr, const R* mi, const R* vr, const R* vi, R& orr, R& oi) {
+  R x = mr[0] * vr[0], y = mr[0] * vi[0];
+  x = fma(-mi[0], vi[0], x);
+  y = fma(mi[0], vr[0], y);
+#pragma unroll
+  for (int c = 1; c < 4; ++c) {
+    x = fma(mr[c], vr[c], x);
+    x = fma(-mi[c], vi[c], x);
+    y = fma(mr[c], vi[c], y);
+    y = fma(mi[c], vr[c], y);
+  }
+  orr = x;
+  oi = y;
+}
+#endif
 
 // ---- launchers (native kernels, k_gates.cu) ----
 template <typename R> void launch_1q(iqsg_state* h, unsigned pos, const M2<R>& m);
@@ -86,5 +132,8 @@ template <typename R> void reduce_max_real(iqsg_state* h);
 
 // ---- emulated-FP64 gate kernels (k_emul.cu) ----
 void launch_1q_emulated(iqsg_state* h, unsigned pos, const M2<double>& m);
+
+// ---- fused sweeps (k_sweep.cu) ----
+unsigned sweep_width(const iqsg_state* h);
 
 }  // namespace iqsg

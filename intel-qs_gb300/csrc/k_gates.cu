@@ -12,8 +12,7 @@ namespace {
 template <typename V, typename R>
 __device__ __forceinline__ V cmul(R mr, R mi, V a) {
   V r;
-  r.x = mr * a.x - mi * a.y;
-  r.y = mr * a.y + mi * a.x;
+  cmul_fma<R>(mr, mi, a.x, a.y, r.x, r.y);
   return r;
 }
 
@@ -21,8 +20,7 @@ __device__ __forceinline__ V cmul(R mr, R mi, V a) {
 template <typename V, typename R>
 __device__ __forceinline__ V row2(const M2<R>& m, int r, V a, V b) {
   V o;
-  o.x = m.re[2 * r] * a.x - m.im[2 * r] * a.y + m.re[2 * r + 1] * b.x - m.im[2 * r + 1] * b.y;
-  o.y = m.re[2 * r] * a.y + m.im[2 * r] * a.x + m.re[2 * r + 1] * b.y + m.im[2 * r + 1] * b.x;
+  row2_fma<R>(m.re[2 * r], m.im[2 * r], m.re[2 * r + 1], m.im[2 * r + 1], a.x, a.y, b.x, b.y, o.x, o.y);
   return o;
 }
 
@@ -161,16 +159,11 @@ __global__ void __launch_bounds__(kThreads) k_2q(typename V2<R>::type* __restric
     V v[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) v[k] = s[idx[k]];
+    const R vr[4] = {v[0].x, v[1].x, v[2].x, v[3].x}, vi[4] = {v[0].y, v[1].y, v[2].y, v[3].y};
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       V o;
-      o.x = m.re[4 * t] * v[0].x - m.im[4 * t] * v[0].y;
-      o.y = m.re[4 * t] * v[0].y + m.im[4 * t] * v[0].x;
-#pragma unroll
-      for (int c = 1; c < 4; ++c) {
-        o.x += m.re[4 * t + c] * v[c].x - m.im[4 * t + c] * v[c].y;
-        o.y += m.re[4 * t + c] * v[c].y + m.im[4 * t + c] * v[c].x;
-      }
+      row4_fma<R>(m.re + 4 * t, m.im + 4 * t, vr, vi, o.x, o.y);
       s[idx[t]] = o;
     }
   }

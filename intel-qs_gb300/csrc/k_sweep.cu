@@ -1,0 +1,620 @@
+// Fused-sweep kernel and the scheduler that packs a gate stream into sweeps (iqsg_apply_ops).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "bulk.cuh"
+#include "sweep.cuh"
+
+namespace iqsg {
+
+namespace {
+
+__device__ __forceinline__ uint64_t gtid() { return (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ uint64_t gstride() { return (uint64_t)gridDim.x * blockDim.x; }
+
+template <int K>
+__device__ __forceinline__ void group_indices(const SweepParams& P, uint64_t g, uint64_t* idx) {
+  uint64_t base = g;
+#pragma unroll
+  for (int k = 0; k < K; ++k) base = insert_zero(base, P.sorted[k]);
+#pragma unroll
+  for (int s = 0; s < (1 << K); ++s) {
+    uint64_t off = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if (s & (1 << j)) off |= uint64_t(1) << P.pos[j];
+    idx[s] = base | off;
+  }
+}
+
+// IEEE arithmetic in the storage precision.
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_sweep_native(typename V2<R>::type* __restrict__ s, uint64_t ngroups,
+                                                           const __grid_constant__ SweepParams P) {
+  constexpr int G = 1 << K;
+  using A = NativeArith<R>;
+  for (uint64_t g = gtid(); g < ngroups; g += gstride()) {
+    uint64_t idx[G];
+    group_indices<K>(P, g, idx);
+    typename A::VT v[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const auto a = s[idx[k]];
+      v[k].re = a.x;
+      v[k].im = a.y;
+    }
+    unsigned tm = 0;
+    run_ops<A, K>(P, v, idx, tm);
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      if (!(tm & (1u << k))) continue;
+      typename V2<R>::type a;
+      a.x = v[k].re;
+      a.y = v[k].im;
+      s[idx[k]] = a;
+    }
+  }
+}
+
+// FP64 storage, double-float arithmetic; a group with a value outside the fast range is
+// recomputed in native FP64. Untouched slots are not rewritten.
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_sweep_df(double2* __restrict__ s, uint64_t ngroups,
+                                                       const __grid_constant__ SweepParams P) {
+  constexpr int G = 1 << K;
+  for (uint64_t g = gtid(); g < ngroups; g += gstride()) {
+    uint64_t idx[G];
+    group_indices<K>(P, g, idx);
+    double2 raw[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) raw[k] = s[idx[k]];
+    DF64Arith::VT v[G];
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      ok &= df64::split(raw[k].x, v[k].re);
+      ok &= df64::split(raw[k].y, v[k].im);
+    }
+    unsigned tm = 0;
+    double2 out[G];
+    if (ok) {
+      run_ops<DF64Arith, K>(P, v, idx, tm);
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        if (tm & (1u << k)) {
+          ok &= df64::merge(v[k].re.h, v[k].re.l, out[k].x);
+          ok &= df64::merge(v[k].im.h, v[k].im.l, out[k].y);
+        }
+      }
+    }
+    if (!ok) {
+      NativeArith<double>::VT w[G];
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        w[k].re = raw[k].x;
+        w[k].im = raw[k].y;
+      }
+      tm = 0;
+      run_ops<NativeArith<double>, K>(P, w, idx, tm);
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        out[k].x = w[k].re;
+        out[k].y = w[k].im;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < G; ++k)
+      if (tm & (1u << k)) s[idx[k]] = out[k];
+  }
+}
+
+// ---- bulk-copy pipelined sweep (large registers) ------------------------------------------
+//
+// A persistent grid streams tiles through shared memory: thread 0 keeps kTmaStages - 1 tiles
+// in flight with cp.async.bulk copies that complete on per-stage mbarriers, while all 256
+// threads apply the sweep to the tile that has landed (one group of 2^K amplitudes each) and
+// store the results straight to global memory. A tile is 2^kh contiguous chunks of T = 2^t
+// amplitudes: the active positions below t lie inside a chunk, those at or above t select the
+// chunk. t = 8 + kl (kl = number of active positions below t), so a tile holds exactly 256
+// groups. Memory latency is hidden by the copies in flight instead of by warps.
+
+constexpr int kTmaThreads = 256;
+constexpr int kTmaStages = 3;
+
+struct TileGeom {
+  unsigned t, kh, kl;
+  unsigned hi_sorted[kSweepMaxK];  // active positions >= t, ascending
+  unsigned lo_sorted[kSweepMaxK];  // active positions < t, ascending
+  uint64_t chunk_off[1 << kSweepMaxK];
+  uint32_t slot_chunk[1 << kSweepMaxK];
+  uint32_t slot_lowoff[1 << kSweepMaxK];
+  uint64_t slot_off[1 << kSweepMaxK];
+};
+
+template <typename R, bool DF, int K>
+__global__ void __launch_bounds__(kTmaThreads) k_sweep_bulk(typename V2<R>::type* __restrict__ s, uint64_t ntiles,
+                                                            const __grid_constant__ TileGeom geo,
+                                                            const __grid_constant__ SweepParams P,
+                                                            unsigned long long* __restrict__ err) {
+  using V = typename V2<R>::type;
+  constexpr int G = 1 << K;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full[kTmaStages];
+  V* sm = reinterpret_cast<V*>(smem_raw);
+  const uint32_t T = 1u << geo.t;
+  const uint32_t nchunks = 1u << geo.kh;
+  const uint32_t chunk_bytes = T * (uint32_t)sizeof(V);
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kTmaStages; ++i) mbar_init(&full[i], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  const uint64_t first = blockIdx.x, stride = gridDim.x;
+  const uint64_t mine = first < ntiles ? (ntiles - 1 - first) / stride + 1 : 0;
+
+  auto tile_base = [&](uint64_t tile) {
+    uint64_t b = tile << geo.t;
+    for (unsigned k = 0; k < geo.kh; ++k) b = insert_zero(b, geo.hi_sorted[k]);
+    return b;
+  };
+  auto issue = [&](uint64_t j) {  // j-th tile of this CTA into stage j % kTmaStages
+    const int st = (int)(j % kTmaStages);
+    const uint64_t tb = tile_base(first + j * stride);
+    mbar_arrive_expect_tx(&full[st], chunk_bytes * nchunks);
+    for (uint32_t c = 0; c < nchunks; ++c)
+      bulk_g2s(sm + (size_t)(st * nchunks + c) * T, s + (tb | geo.chunk_off[c]), chunk_bytes, &full[st]);
+  };
+
+  uint64_t issued = 0;
+  if (threadIdx.x == 0)
+    for (; issued < (uint64_t)(kTmaStages - 1) && issued < mine; ++issued) issue(issued);
+
+  uint64_t lb = threadIdx.x;
+  for (unsigned k = 0; k < geo.kl; ++k) lb = insert_zero(lb, geo.lo_sorted[k]);
+
+  uint64_t i = 0;
+  bool failed = false;
+  for (; i < mine; ++i) {
+    const int st = (int)(i % kTmaStages);
+    if (threadIdx.x == 0 && issued < mine) {
+      // The stage refilled here held tile i - 1, whose reads ended at the barrier below.
+      fence_proxy_async_smem();
+      issue(issued++);
+    }
+    const bool ok_wait = mbar_wait(&full[st], (uint32_t)((i / kTmaStages) & 1));
+    if (ok_wait) {
+      const uint64_t tb = tile_base(first + i * stride) | lb;
+      const V* stage = sm + (size_t)st * nchunks * T;
+      uint64_t idx[G];
+      V raw[G];
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        idx[k] = tb | geo.slot_off[k];
+        raw[k] = stage[(size_t)geo.slot_chunk[k] * T + (lb | geo.slot_lowoff[k])];
+      }
+      unsigned tm = 0;
+      if constexpr (DF) {
+        DF64Arith::VT v[G];
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+          ok &= df64::split(raw[k].x, v[k].re);
+          ok &= df64::split(raw[k].y, v[k].im);
+        }
+        V out[G];
+        if (ok) {
+          run_ops<DF64Arith, K>(P, v, idx, tm);
+#pragma unroll
+          for (int k = 0; k < G; ++k)
+            if (tm & (1u << k)) {
+              ok &= df64::merge(v[k].re.h, v[k].re.l, out[k].x);
+              ok &= df64::merge(v[k].im.h, v[k].im.l, out[k].y);
+            }
+        }
+        if (!ok) {
+          NativeArith<double>::VT w[G];
+#pragma unroll
+          for (int k = 0; k < G; ++k) {
+            w[k].re = raw[k].x;
+            w[k].im = raw[k].y;
+          }
+          tm = 0;
+          run_ops<NativeArith<double>, K>(P, w, idx, tm);
+#pragma unroll
+          for (int k = 0; k < G; ++k) {
+            out[k].x = w[k].re;
+            out[k].y = w[k].im;
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < G; ++k)
+          if (tm & (1u << k)) s[idx[k]] = out[k];
+      } else {
+        typename NativeArith<R>::VT v[G];
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+          v[k].re = raw[k].x;
+          v[k].im = raw[k].y;
+        }
+        run_ops<NativeArith<R>, K>(P, v, idx, tm);
+#pragma unroll
+        for (int k = 0; k < G; ++k)
+          if (tm & (1u << k)) {
+            V a;
+            a.x = v[k].re;
+            a.y = v[k].im;
+            s[idx[k]] = a;
+          }
+      }
+    }
+    // Block-uniform decision: every thread reaches this barrier each iteration.
+    if (__syncthreads_or(!ok_wait)) {
+      failed = true;
+      break;
+    }
+  }
+  if (failed && threadIdx.x == 0) {
+    atomicExch(err, 1ull);
+    // Let the copies this CTA still has in flight land (bounded) before it exits.
+    for (uint64_t j = i; j < issued; ++j) (void)mbar_wait(&full[j % kTmaStages], (uint32_t)((j / kTmaStages) & 1));
+  }
+}
+
+bool make_geometry(const SweepParams& P, unsigned n, TileGeom& g) {
+  const unsigned K = P.K;
+  unsigned kl = 0;
+  for (; kl <= K; ++kl) {
+    unsigned below = 0;
+    for (unsigned j = 0; j < K; ++j) below += P.pos[j] < 8 + kl ? 1u : 0u;
+    if (below == kl) break;
+  }
+  if (kl > K) return false;
+  std::memset(&g, 0, sizeof g);
+  g.t = 8 + kl;
+  g.kl = kl;
+  g.kh = K - kl;
+  if (n < g.t + g.kh) return false;
+  unsigned nh = 0, nl = 0;
+  for (unsigned j = 0; j < K; ++j) {
+    if (P.sorted[j] >= g.t) g.hi_sorted[nh++] = P.sorted[j];
+    else g.lo_sorted[nl++] = P.sorted[j];
+  }
+  for (unsigned c = 0; c < (1u << g.kh); ++c)
+    for (unsigned b = 0; b < g.kh; ++b)
+      if (c & (1u << b)) g.chunk_off[c] |= uint64_t(1) << g.hi_sorted[b];
+  for (unsigned sl = 0; sl < (1u << K); ++sl) {
+    uint32_t chunk = 0, low = 0;
+    for (unsigned j = 0; j < K; ++j) {
+      if (!(sl & (1u << j))) continue;
+      const unsigned p = P.pos[j];
+      if (p >= g.t) {
+        unsigned rank = 0;
+        while (g.hi_sorted[rank] != p) ++rank;
+        chunk |= 1u << rank;
+      } else {
+        low |= 1u << p;
+      }
+    }
+    g.slot_chunk[sl] = chunk;
+    g.slot_lowoff[sl] = low;
+    g.slot_off[sl] = g.chunk_off[chunk] | low;
+  }
+  return true;
+}
+
+template <typename R, bool DF, int K>
+void launch_bulk(iqsg_state* h, const SweepParams& P, const TileGeom& g) {
+  using V = typename V2<R>::type;
+  const size_t smem = (size_t)kTmaStages * (size_t(256) << K) * sizeof(V);
+  static int blocks_per_sm = -1;  // per instantiation
+  if (blocks_per_sm < 0) {
+    cudaFuncSetAttribute(k_sweep_bulk<R, DF, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_sweep_bulk<R, DF, K>, kTmaThreads, smem) != cudaSuccess ||
+        b < 1)
+      b = 1;
+    blocks_per_sm = b;
+  }
+  const uint64_t ntiles = h->N >> (K + 8);
+  uint64_t grid = (uint64_t)num_sms() * (uint64_t)blocks_per_sm;
+  if (grid > ntiles) grid = ntiles;
+  k_sweep_bulk<R, DF, K><<<(unsigned)grid, kTmaThreads, smem, h->stream>>>(
+      reinterpret_cast<V*>(h->amps), ntiles, g, P, reinterpret_cast<unsigned long long*>(h->scratch + kErrorSlot));
+}
+
+template <int K>
+void launch_k(iqsg_state* h, const SweepParams& P) {
+  const uint64_t ngroups = h->N >> K;
+  const bool df = h->prec == IQSG_COMPLEX_DP && h->math == IQSG_MATH_EMULATED && K <= 3;
+  TileGeom g;
+  if (h->n >= kBulkMinQubits && !h->no_bulk && make_geometry(P, h->n, g)) {
+    if (h->prec == IQSG_COMPLEX_SP) launch_bulk<float, false, K>(h, P, g);
+    else if (df) launch_bulk<double, (K <= 3), K>(h, P, g);
+    else launch_bulk<double, false, K>(h, P, g);
+    return;
+  }
+  const unsigned grid = grid_for(ngroups, 1);
+  if (h->prec == IQSG_COMPLEX_SP) {
+    k_sweep_native<float, K><<<grid, kThreads, 0, h->stream>>>(reinterpret_cast<float2*>(h->amps), ngroups, P);
+  } else if (df) {
+    if constexpr (K <= 3) {
+      k_sweep_df<K><<<grid, kThreads, 0, h->stream>>>(reinterpret_cast<double2*>(h->amps), ngroups, P);
+    }
+  } else {
+    k_sweep_native<double, K><<<grid, kThreads, 0, h->stream>>>(reinterpret_cast<double2*>(h->amps), ngroups, P);
+  }
+}
+
+}  // namespace
+
+void launch_sweep(iqsg_state* h, const SweepParams& P) {
+  switch (P.K) {
+    case 0: launch_k<0>(h, P); break;
+    case 1: launch_k<1>(h, P); break;
+    case 2: launch_k<2>(h, P); break;
+    case 3: launch_k<3>(h, P); break;
+    case 4: launch_k<4>(h, P); break;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Scheduler: greedy packing of a gate stream into sweeps.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+bool is_one(double re, double im) { return re == 1.0 && im == 0.0; }
+bool is_zero(double re, double im) { return re == 0.0 && im == 0.0; }
+
+SweepEntry make_entry(double re, double im) {
+  SweepEntry e;
+  e.re = re;
+  e.im = im;
+  const df64::DF r = df64::split_host(re), i = df64::split_host(im);
+  e.rh = r.h;
+  e.rl = r.l;
+  e.ih = i.h;
+  e.il = i.l;
+  return e;
+}
+
+uint8_t phase_flags(double re, double im) {
+  if (re == -1.0 && im == 0.0) return SF_NEG;
+  if (re == 0.0 && im == 1.0) return SF_ONE_I;
+  if (re == 0.0 && im == -1.0) return SF_NEG_I;
+  return SF_NONE;
+}
+
+bool is_x(const double* m) {
+  return is_zero(m[0], m[1]) && is_one(m[2], m[3]) && is_one(m[4], m[5]) && is_zero(m[6], m[7]);
+}
+
+class SweepBuilder {
+ public:
+  SweepBuilder(iqsg_state* h, unsigned kmax) : h_(h), kmax_(kmax) { reset(); }
+
+  // Slot of position p in the current sweep, or -1 when p is not active.
+  int slot(unsigned p) {
+    for (unsigned j = 0; j < P_.K; ++j)
+      if (P_.pos[j] == p) return (int)j;
+    return -1;
+  }
+
+  bool fits(const std::vector<unsigned>& targets, unsigned ops, unsigned entries) const {
+    unsigned add = 0;
+    for (unsigned t : targets) {
+      bool have = false;
+      for (unsigned j = 0; j < P_.K; ++j) have = have || P_.pos[j] == t;
+      add += have ? 0u : 1u;
+    }
+    // A two-position operation opens a 2-wide sweep even when the width limit is 1.
+    const unsigned kmax = std::max<unsigned>(kmax_, (unsigned)targets.size());
+    return P_.K + add <= kmax && P_.nops + ops <= (unsigned)kSweepMaxOps &&
+           nent_ + entries <= (unsigned)kSweepMaxEntries;
+  }
+
+  // Make room (flushing if necessary) and activate the target positions.
+  void reserve(const std::vector<unsigned>& targets, unsigned ops, unsigned entries) {
+    if (!fits(targets, ops, entries)) flush();
+    for (unsigned t : targets)
+      if (slot(t) < 0) P_.pos[P_.K++] = t;
+  }
+
+  uint16_t add_entries(const double* m, unsigned count) {
+    const uint16_t first = (uint16_t)nent_;
+    for (unsigned k = 0; k < count; ++k) P_.ent[nent_++] = make_entry(m[2 * k], m[2 * k + 1]);
+    return first;
+  }
+
+  void add_phase(uint64_t mask, uint64_t value, double re, double im) {
+    if (is_one(re, im)) return;
+    reserve({}, 1, 1);
+    SweepOp op{};
+    op.kind = SW_PHASE;
+    op.mask = mask;
+    op.value = value;
+    op.flags = phase_flags(re, im);
+    const double e[2] = {re, im};
+    op.ent = add_entries(e, 1);
+    P_.ops[P_.nops++] = op;
+  }
+
+  // 2x2 on target t where all bits of cmask are 1 (cmask excludes t).
+  void add_u2(unsigned t, uint64_t cmask, const double* m) {
+    const uint64_t tb = uint64_t(1) << t;
+    if (is_zero(m[2], m[3]) && is_zero(m[4], m[5])) {  // diagonal: phases only
+      add_phase(cmask | tb, cmask, m[0], m[1]);
+      add_phase(cmask | tb, cmask | tb, m[6], m[7]);
+      return;
+    }
+    reserve({t}, 1, 4);
+    SweepOp op{};
+    op.kind = SW_U2;
+    op.mask = cmask;
+    op.j0 = (uint8_t)slot(t);
+    op.flags = is_x(m) ? SF_X : SF_NONE;
+    op.ent = add_entries(m, 4);
+    P_.ops[P_.nops++] = op;
+  }
+
+  void add_u4(unsigned ph, unsigned pl, const double* m) {
+    bool diag = true;
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c)
+        if (r != c && !is_zero(m[2 * (4 * r + c)], m[2 * (4 * r + c) + 1])) diag = false;
+    const uint64_t bh = uint64_t(1) << ph, bl = uint64_t(1) << pl;
+    if (diag) {
+      for (int k = 0; k < 4; ++k)
+        add_phase(bh | bl, ((k & 2) ? bh : 0) | ((k & 1) ? bl : 0), m[2 * (5 * k)], m[2 * (5 * k) + 1]);
+      return;
+    }
+    reserve({ph, pl}, 1, 16);
+    SweepOp op{};
+    op.kind = SW_U4;
+    op.j0 = (uint8_t)slot(ph);
+    op.j1 = (uint8_t)slot(pl);
+    op.ent = add_entries(m, 16);
+    P_.ops[P_.nops++] = op;
+  }
+
+  void add_swaplike(unsigned p1, unsigned p2, const double* m) {
+    const unsigned lo = std::min(p1, p2), hi = std::max(p1, p2);
+    reserve({lo, hi}, 1, 4);
+    SweepOp op{};
+    op.kind = SW_SWAPLIKE;
+    op.j0 = (uint8_t)slot(lo);
+    op.j1 = (uint8_t)slot(hi);
+    op.flags = is_x(m) ? SF_X : SF_NONE;
+    op.ent = add_entries(m, 4);
+    P_.ops[P_.nops++] = op;
+  }
+
+  void flush() {
+    if (P_.nops) {
+      std::copy(P_.pos, P_.pos + P_.K, P_.sorted);
+      std::sort(P_.sorted, P_.sorted + P_.K);
+      launch_sweep(h_, P_);
+      ++launched_;
+    }
+    reset();
+  }
+
+  unsigned launched() const { return launched_; }
+
+ private:
+  void reset() {
+    std::memset(&P_, 0, sizeof(P_));
+    nent_ = 0;
+  }
+  iqsg_state* h_;
+  unsigned kmax_;
+  SweepParams P_;
+  unsigned nent_ = 0;
+  unsigned launched_ = 0;
+};
+
+unsigned default_width(const iqsg_state* h) {
+  if (h->prec == IQSG_COMPLEX_SP) return 4;
+  return h->math == IQSG_MATH_EMULATED ? 2 : 3;
+}
+
+}  // namespace
+
+unsigned sweep_width(const iqsg_state* h) {
+  unsigned k = h->sweep_width ? h->sweep_width : default_width(h);
+  if (h->prec == IQSG_COMPLEX_DP && h->math == IQSG_MATH_EMULATED && k > 3) k = 3;
+  return std::min(k, std::min(h->n, (unsigned)kSweepMaxK));
+}
+
+}  // namespace iqsg
+
+using namespace iqsg;
+
+namespace {
+
+int check_op(const iqsg_state* h, const iqsg_op& op, unsigned i) {
+  auto bad = [&](const char* why) { return fail(IQSG_EINVAL, "iqsg_apply_ops: op %u: %s", i, why); };
+  uint64_t seen = 0;
+  auto use = [&](unsigned p) {
+    if (p >= h->n) return false;
+    if (seen & (uint64_t(1) << p)) return false;
+    seen |= uint64_t(1) << p;
+    return true;
+  };
+  switch (op.kind) {
+    case IQSG_OP_1Q:
+      if (!use(op.t0)) return bad("target out of range");
+      break;
+    case IQSG_OP_CTRL:
+      if (op.nctrl > 4) return bad("more than 4 controls");
+      for (unsigned c = 0; c < op.nctrl; ++c)
+        if (!use(op.ctrl[c])) return bad("control out of range or repeated");
+      if (!use(op.t0)) return bad("target out of range or equal to a control");
+      break;
+    case IQSG_OP_2Q:
+    case IQSG_OP_SWAPLIKE:
+    case IQSG_OP_DIAG2:
+      if (!use(op.t0) || !use(op.t1)) return bad("positions out of range or equal");
+      break;
+    case IQSG_OP_PHASE:
+      if (h->n < 64 && ((op.mask >> h->n) != 0)) return bad("phase mask beyond the register");
+      if ((op.value & ~op.mask) != 0) return bad("phase value outside its mask");
+      break;
+    default:
+      return bad("unknown kind");
+  }
+  return IQSG_OK;
+}
+
+}  // namespace
+
+extern "C" int iqsg_set_sweep_width(iqsg_state* h, unsigned kmax) {
+  if (!h) return fail(IQSG_EINVAL, "null register handle");
+  if (kmax > (unsigned)kSweepMaxK) return fail(IQSG_EINVAL, "iqsg_set_sweep_width: width %u above %d", kmax, kSweepMaxK);
+  h->sweep_width = kmax;
+  return IQSG_OK;
+}
+
+extern "C" int iqsg_apply_ops(iqsg_state* h, const iqsg_op* ops, unsigned count, unsigned* sweeps) {
+  if (!h) return fail(IQSG_EINVAL, "null register handle");
+  if (count && !ops) return fail(IQSG_EINVAL, "iqsg_apply_ops: null op array");
+  for (unsigned i = 0; i < count; ++i) {
+    const int st = check_op(h, ops[i], i);
+    if (st) return st;
+  }
+  SweepBuilder b(h, std::max(1u, sweep_width(h)));
+  for (unsigned i = 0; i < count; ++i) {
+    const iqsg_op& op = ops[i];
+    switch (op.kind) {
+      case IQSG_OP_1Q:
+        b.add_u2(op.t0, 0, op.m);
+        break;
+      case IQSG_OP_CTRL: {
+        uint64_t cm = 0;
+        for (unsigned c = 0; c < op.nctrl; ++c) cm |= uint64_t(1) << op.ctrl[c];
+        b.add_u2(op.t0, cm, op.m);
+        break;
+      }
+      case IQSG_OP_2Q:
+        b.add_u4(op.t0, op.t1, op.m);
+        break;
+      case IQSG_OP_SWAPLIKE:
+        b.add_swaplike(op.t0, op.t1, op.m);
+        break;
+      case IQSG_OP_DIAG2: {
+        const uint64_t b1 = uint64_t(1) << op.t0, b2 = uint64_t(1) << op.t1;
+        for (int k = 0; k < 4; ++k)
+          b.add_phase(b1 | b2, ((k & 2) ? b1 : 0) | ((k & 1) ? b2 : 0), op.m[2 * k], op.m[2 * k + 1]);
+        break;
+      }
+      case IQSG_OP_PHASE:
+        b.add_phase(op.mask, op.value, op.m[0], op.m[1]);
+        break;
+    }
+  }
+  b.flush();
+  if (sweeps) *sweeps = b.launched();
+  return cuda_status(cudaGetLastError(), "iqsg_apply_ops");
+}

@@ -1,0 +1,315 @@
+// Fused sweeps: one pass over the state that applies an ordered list of gate operations.
+//
+// A sweep has K "active" positions (0 <= K <= 4). Each thread owns groups of 2^K amplitudes:
+// the indices that differ only in the active bits. Non-diagonal operations act inside a
+// group (2x2 on one active bit, 4x4 or swap-type on two), so the group is loaded once,
+// every operation is applied in registers in program order, and the group is stored once.
+// Diagonal operations (phases, controlled phases, CZ, the ApplyDiag entries) act on single
+// amplitudes selected by their index bits and may involve any position, active or not.
+// Control bits may sit on any position too. Applying the list group by group gives exactly
+// the result of applying it operation by operation, because a group is closed under every
+// operation of the sweep.
+#pragma once
+
+#include "df64.cuh"
+#include "iqsg_internal.cuh"
+
+namespace iqsg {
+
+constexpr int kSweepMaxK = 4;
+constexpr int kSweepMaxOps = 48;
+constexpr int kSweepMaxEntries = 160;
+
+enum SweepKind : uint8_t {
+  SW_U2 = 0,        // 2x2 on active bit j0, applied where (idx & mask) == mask
+  SW_PHASE = 1,     // amp *= entry where (idx & mask) == value
+  SW_U4 = 2,        // 4x4 on active bits (j0 = high, j1 = low), where (idx & mask) == mask
+  SW_SWAPLIKE = 3,  // 2x2 on the (j0 = 1, j1 = 0) / (j0 = 0, j1 = 1) pair, where (idx & mask) == mask
+};
+
+enum SweepFlags : uint8_t {
+  SF_NONE = 0,
+  SF_NEG = 1,    // PHASE by -1: exact sign flip
+  SF_X = 2,      // U2/SWAPLIKE with m = [[0,1],[1,0]]: exact exchange
+  SF_ONE_I = 4,  // PHASE by +i: exact (re, im) -> (-im, re)
+  SF_NEG_I = 8,  // PHASE by -i: exact (re, im) -> (im, -re)
+};
+
+struct SweepOp {
+  uint64_t mask, value;
+  uint16_t ent;  // first matrix entry
+  uint8_t kind, flags;
+  uint8_t j0, j1;
+  uint8_t pad[2];
+};
+
+// One complex matrix entry in both representations: native (re, im) in the register's
+// precision, and the double-float split used by the emulated path.
+struct SweepEntry {
+  double re, im;
+  float rh, rl, ih, il;
+};
+
+struct SweepParams {
+  unsigned K;
+  unsigned pos[kSweepMaxK];     // active slot bit j <-> position pos[j]
+  unsigned sorted[kSweepMaxK];  // active positions ascending (zero insertion)
+  unsigned nops;
+  SweepOp ops[kSweepMaxOps];
+  SweepEntry ent[kSweepMaxEntries];
+};
+
+// ---- arithmetic policies -----------------------------------------------------------------
+
+// IEEE arithmetic in R (double or float): the same formulas as the per-gate kernels.
+template <typename R>
+struct NativeArith {
+  struct VT {
+    R re, im;
+  };
+  // FP32 uses the float head of the entry, which is the double rounded to nearest float
+  // (no double -> float conversion on the device).
+  __device__ static __forceinline__ R re_of(const SweepEntry& e) {
+    if constexpr (sizeof(R) == 4) return e.rh;
+    else return e.re;
+  }
+  __device__ static __forceinline__ R im_of(const SweepEntry& e) {
+    if constexpr (sizeof(R) == 4) return e.ih;
+    else return e.im;
+  }
+  // r0 = m0 a + m1 b
+  __device__ static __forceinline__ VT row(const SweepEntry& m0, const SweepEntry& m1, const VT& a, const VT& b) {
+    VT o;
+    row2_fma<R>(re_of(m0), im_of(m0), re_of(m1), im_of(m1), a.re, a.im, b.re, b.im, o.re, o.im);
+    return o;
+  }
+  __device__ static __forceinline__ VT mul(const SweepEntry& f, const VT& a) {
+    VT o;
+    cmul_fma<R>(re_of(f), im_of(f), a.re, a.im, o.re, o.im);
+    return o;
+  }
+  // row of a 4x4: sum_c m_c v_c
+  __device__ static __forceinline__ VT row4(const SweepEntry* m, const VT* v) {
+    R mr[4], mi[4], vr[4], vi[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      mr[c] = re_of(m[c]);
+      mi[c] = im_of(m[c]);
+      vr[c] = v[c].re;
+      vi[c] = v[c].im;
+    }
+    VT o;
+    row4_fma<R>(mr, mi, vr, vi, o.re, o.im);
+    return o;
+  }
+};
+
+// Double-float arithmetic on FP64 data (see df64.cuh); VT holds (h, l) pairs.
+struct DF64Arith {
+  struct VT {
+    df64::DF re, im;
+  };
+  // sum of n double-float products c_k * x_k, c given as (h, l) constants
+  template <int NT>
+  __device__ static __forceinline__ df64::DF dot(const float* ch, const float* cl, const df64::DF* x) {
+    float ph, pl;
+    df64::Acc s;
+    df64::prod(ch[0], cl[0], x[0].h, x[0].l, ph, pl);
+    df64::acc_init(s, ph, pl);
+#pragma unroll
+    for (int k = 1; k < NT; ++k) {
+      df64::prod(ch[k], cl[k], x[k].h, x[k].l, ph, pl);
+      df64::acc_add(s, ph, pl);
+    }
+    df64::DF r;
+    r.h = df64::add_rn(s.h, s.l);  // Fast2Sum renormalisation: |s.l| << |s.h|
+    r.l = df64::sub_rn(s.l, df64::sub_rn(r.h, s.h));
+    return r;
+  }
+  __device__ static __forceinline__ VT row(const SweepEntry& m0, const SweepEntry& m1, const VT& a, const VT& b) {
+    const float reh[4] = {m0.rh, -m0.ih, m1.rh, -m1.ih}, rel[4] = {m0.rl, -m0.il, m1.rl, -m1.il};
+    const float imh[4] = {m0.rh, m0.ih, m1.rh, m1.ih}, iml[4] = {m0.rl, m0.il, m1.rl, m1.il};
+    const df64::DF xr[4] = {a.re, a.im, b.re, b.im};
+    const df64::DF xi[4] = {a.im, a.re, b.im, b.re};
+    VT o;
+    o.re = dot<4>(reh, rel, xr);
+    o.im = dot<4>(imh, iml, xi);
+    return o;
+  }
+  __device__ static __forceinline__ VT mul(const SweepEntry& f, const VT& a) {
+    const float reh[2] = {f.rh, -f.ih}, rel[2] = {f.rl, -f.il};
+    const float imh[2] = {f.rh, f.ih}, iml[2] = {f.rl, f.il};
+    const df64::DF xr[2] = {a.re, a.im}, xi[2] = {a.im, a.re};
+    VT o;
+    o.re = dot<2>(reh, rel, xr);
+    o.im = dot<2>(imh, iml, xi);
+    return o;
+  }
+  __device__ static __forceinline__ VT row4(const SweepEntry* m, const VT* v) {
+    float reh[8], rel[8], imh[8], iml[8];
+    df64::DF xr[8], xi[8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      reh[2 * c] = m[c].rh; rel[2 * c] = m[c].rl; reh[2 * c + 1] = -m[c].ih; rel[2 * c + 1] = -m[c].il;
+      imh[2 * c] = m[c].rh; iml[2 * c] = m[c].rl; imh[2 * c + 1] = m[c].ih; iml[2 * c + 1] = m[c].il;
+      xr[2 * c] = v[c].re; xr[2 * c + 1] = v[c].im;
+      xi[2 * c] = v[c].im; xi[2 * c + 1] = v[c].re;
+    }
+    VT o;
+    o.re = dot<8>(reh, rel, xr);
+    o.im = dot<8>(imh, iml, xi);
+    return o;
+  }
+};
+
+// ---- exact operations common to both ----------------------------------------------------
+__device__ __forceinline__ double cneg(double x) { return -x; }
+__device__ __forceinline__ float cneg(float x) { return -x; }
+__device__ __forceinline__ df64::DF cneg(df64::DF x) {
+  x.h = -x.h;
+  x.l = -x.l;
+  return x;
+}
+template <typename VT>
+__device__ __forceinline__ void vt_neg(VT& a) {
+  a.re = cneg(a.re);
+  a.im = cneg(a.im);
+}
+// Multiply by +i: (re, im) -> (-im, re); by -i: (re, im) -> (im, -re). Exact.
+template <typename VT>
+__device__ __forceinline__ void vt_mul_i(VT& a, bool plus) {
+  const auto re = a.re;
+  if (plus) {
+    a.re = cneg(a.im);
+    a.im = re;
+  } else {
+    a.re = a.im;
+    a.im = cneg(re);
+  }
+}
+
+// ---- the op interpreter -----------------------------------------------------------------
+
+template <typename A, int K, int J>
+__device__ __forceinline__ void op_u2(const SweepParams& P, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
+                                      unsigned& tm) {
+  constexpr int G = 1 << K, B = 1 << J;
+  const SweepEntry* m = P.ent + op.ent;
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if (s & B) continue;
+    if ((idx[s] & op.mask) != op.mask) continue;
+    typename A::VT a = v[s], b = v[s | B];
+    tm |= (1u << s) | (1u << (s | B));
+    if (op.flags & SF_X) {
+      v[s] = b;
+      v[s | B] = a;
+    } else {
+      v[s] = A::row(m[0], m[1], a, b);
+      v[s | B] = A::row(m[2], m[3], a, b);
+    }
+  }
+}
+
+template <typename A, int K, int JH, int JL>
+__device__ __forceinline__ void op_u4(const SweepParams& P, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
+                                      unsigned& tm) {
+  constexpr int G = 1 << K, BH = 1 << JH, BL = 1 << JL;
+  const SweepEntry* m = P.ent + op.ent;
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if (s & (BH | BL)) continue;
+    if ((idx[s] & op.mask) != op.mask) continue;
+    const typename A::VT q[4] = {v[s], v[s | BL], v[s | BH], v[s | BH | BL]};
+    tm |= (1u << s) | (1u << (s | BL)) | (1u << (s | BH)) | (1u << (s | BH | BL));
+    v[s] = A::row4(m, q);
+    v[s | BL] = A::row4(m + 4, q);
+    v[s | BH] = A::row4(m + 8, q);
+    v[s | BH | BL] = A::row4(m + 12, q);
+  }
+}
+
+template <typename A, int K, int JLO, int JHI>
+__device__ __forceinline__ void op_swaplike(const SweepParams& P, const SweepOp& op, typename A::VT* v,
+                                            const uint64_t* idx, unsigned& tm) {
+  constexpr int G = 1 << K, BL = 1 << JLO, BH = 1 << JHI;
+  const SweepEntry* m = P.ent + op.ent;
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if (s & (BH | BL)) continue;
+    if ((idx[s] & op.mask) != op.mask) continue;
+    typename A::VT a = v[s | BL], b = v[s | BH];
+    tm |= (1u << (s | BL)) | (1u << (s | BH));
+    if (op.flags & SF_X) {
+      v[s | BL] = b;
+      v[s | BH] = a;
+    } else {
+      v[s | BL] = A::row(m[0], m[1], a, b);
+      v[s | BH] = A::row(m[2], m[3], a, b);
+    }
+  }
+}
+
+template <typename A, int K>
+__device__ __forceinline__ void op_phase(const SweepParams& P, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
+                                         unsigned& tm) {
+  constexpr int G = 1 << K;
+  const SweepEntry& f = P.ent[op.ent];
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if ((idx[s] & op.mask) != op.value) continue;
+    tm |= 1u << s;
+    if (op.flags & SF_NEG) vt_neg(v[s]);
+    else if (op.flags & SF_ONE_I) vt_mul_i(v[s], true);
+    else if (op.flags & SF_NEG_I) vt_mul_i(v[s], false);
+    else v[s] = A::mul(f, v[s]);
+  }
+}
+
+// Apply every operation of the sweep to one group, in order. Bit s of tm records that slot s
+// was written. A runtime active-bit index is dispatched to a compile-time one, so the group
+// stays in registers (no dynamic register indexing).
+template <typename A, int K>
+__device__ __forceinline__ void run_ops(const SweepParams& P, typename A::VT* v, const uint64_t* idx, unsigned& tm) {
+#pragma unroll 1
+  for (unsigned o = 0; o < P.nops; ++o) {
+    const SweepOp op = P.ops[o];
+    switch (op.kind) {
+      case SW_PHASE:
+        op_phase<A, K>(P, op, v, idx, tm);
+        break;
+      case SW_U2:
+        if constexpr (K >= 1) {
+          switch (op.j0) {
+            case 0: op_u2<A, K, 0>(P, op, v, idx, tm); break;
+            case 1: if constexpr (K >= 2) op_u2<A, K, (K >= 2 ? 1 : 0)>(P, op, v, idx, tm); break;
+            case 2: if constexpr (K >= 3) op_u2<A, K, (K >= 3 ? 2 : 0)>(P, op, v, idx, tm); break;
+            case 3: if constexpr (K >= 4) op_u2<A, K, (K >= 4 ? 3 : 0)>(P, op, v, idx, tm); break;
+          }
+        }
+        break;
+      case SW_U4:
+      case SW_SWAPLIKE:
+        if constexpr (K >= 2) {
+          const bool u4 = op.kind == SW_U4;
+          const int a = op.j0, b = op.j1;
+#define IQSG_PAIR_CASE(X, Y)                                                               \
+  if (a == X && b == Y) {                                                                  \
+    if constexpr (K > (X > Y ? X : Y)) {                                                   \
+      if (u4) op_u4<A, K, X, Y>(P, op, v, idx, tm); else op_swaplike<A, K, X, Y>(P, op, v, idx, tm); \
+    }                                                                                      \
+  }
+          IQSG_PAIR_CASE(0, 1) IQSG_PAIR_CASE(1, 0) IQSG_PAIR_CASE(0, 2) IQSG_PAIR_CASE(2, 0)
+          IQSG_PAIR_CASE(1, 2) IQSG_PAIR_CASE(2, 1) IQSG_PAIR_CASE(0, 3) IQSG_PAIR_CASE(3, 0)
+          IQSG_PAIR_CASE(1, 3) IQSG_PAIR_CASE(3, 1) IQSG_PAIR_CASE(2, 3) IQSG_PAIR_CASE(3, 2)
+#undef IQSG_PAIR_CASE
+        }
+        break;
+    }
+  }
+}
+
+// Host side: launch one sweep on the register (k_sweep.cu).
+void launch_sweep(iqsg_state* h, const SweepParams& P);
+
+}  // namespace iqsg

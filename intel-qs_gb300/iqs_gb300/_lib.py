@@ -24,6 +24,17 @@ _DP = C.POINTER(C.c_double)
 _UP = C.POINTER(C.c_uint)
 _IP = C.POINTER(C.c_int)
 
+OP_1Q, OP_CTRL, OP_2Q, OP_SWAPLIKE, OP_DIAG2, OP_PHASE = range(6)
+
+
+class Op(C.Structure):
+    """iqsg_op (include/iqsg.h): one gate of a stream for iqsg_apply_ops."""
+    _fields_ = [("kind", C.c_int32), ("t0", C.c_uint32), ("t1", C.c_uint32), ("nctrl", C.c_uint32),
+                ("ctrl", C.c_uint32 * 4), ("mask", C.c_uint64), ("value", C.c_uint64), ("m", C.c_double * 32)]
+
+
+assert C.sizeof(Op) == 304, "iqsg_op layout mismatch"
+
 # name -> argtypes (every function returns int status unless listed in _RESTYPES)
 SIGNATURES = {
     "iqsg_last_error": [],
@@ -61,6 +72,8 @@ SIGNATURES = {
     "iqsg_l2_diff": [_P, _P, _DP],
     "iqsg_cost_expectation": [_P, _P, C.c_int, _DP],
     "iqsg_maxcut_cost": [_P, _IP, _UP, _IP],
+    "iqsg_apply_ops": [_P, C.POINTER(Op), _U, _UP],
+    "iqsg_set_sweep_width": [_P, _U],
     "iqsg_probability_static": [_P, _U, C.c_int, _U, _P, _P],
 }
 _RESTYPES = {"iqsg_last_error": C.c_char_p}

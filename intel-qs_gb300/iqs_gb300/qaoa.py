@@ -22,6 +22,7 @@ def InitializeVectorAsMaxCutCostFunction(diag: QubitRegister, adjacency: Sequenc
     if adj.size != n * n:
         raise ValueError(f"adjacency must have {n * n} entries, got {adj.size}")
     mp = np.asarray(diag.qubit_permutation.map, dtype=np.uint32)
+    diag._flush()
     mx = C.c_int()
     check(lib.iqsg_maxcut_cost(diag._h, iptr(adj), uptr(mp), C.byref(mx)))
     return mx.value
@@ -31,6 +32,8 @@ def ImplementQaoaLayerBasedOnCostFunction(psi: QubitRegister, diag: QubitRegiste
     """psi[i] *= exp(-i gamma Re diag[i]) (src/qaoa_features.cpp:248-264)."""
     if psi.qubit_permutation.map != diag.qubit_permutation.map:
         raise ValueError("psi and diag have different qubit orders")
+    psi._flush()
+    diag._flush()
     check(lib.iqsg_apply_cost_phase(psi._h, diag._h, psi._bt(gamma)))
 
 
@@ -38,6 +41,8 @@ def GetExpectationValueFromCostFunction(psi: QubitRegister, diag: QubitRegister)
     """sum_i Re diag[i] |psi_i|^2 (src/qaoa_features.cpp:273-300)."""
     if psi.qubit_permutation.map != diag.qubit_permutation.map:
         raise ValueError("psi and diag have different qubit orders")
+    psi._flush()
+    diag._flush()
     v = C.c_double()
     check(lib.iqsg_cost_expectation(psi._h, diag._h, 1, C.byref(v)))
     return v.value
@@ -47,6 +52,8 @@ def GetExpectationValueSquaredFromCostFunction(psi: QubitRegister, diag: QubitRe
     """sum_i (Re diag[i])^2 |psi_i|^2 (src/qaoa_features.cpp:304-331)."""
     if psi.qubit_permutation.map != diag.qubit_permutation.map:
         raise ValueError("psi and diag have different qubit orders")
+    psi._flush()
+    diag._flush()
     v = C.c_double()
     check(lib.iqsg_cost_expectation(psi._h, diag._h, 2, C.byref(v)))
     return v.value

@@ -30,6 +30,18 @@ def _m2(m) -> np.ndarray:
     return a.reshape(-1).view(np.float64).copy()
 
 
+def _op(kind: int, t0: int = 0, t1: int = 0, m=None, ctrl=(), mask: int = 0, value: int = 0) -> "_lib.Op":
+    op = _lib.Op()
+    op.kind, op.t0, op.t1 = kind, t0, t1
+    op.nctrl = len(ctrl)
+    for k, c in enumerate(ctrl):
+        op.ctrl[k] = c
+    op.mask, op.value = mask, value
+    if m is not None:
+        C.memmove(op.m, m.ctypes.data, m.nbytes)
+    return op
+
+
 def _m4(m) -> np.ndarray:
     a = np.ascontiguousarray(np.asarray(m, dtype=np.complex128))
     if a.ndim != 2 or a.shape != (4, 4):
@@ -55,6 +67,7 @@ class QubitRegister:
         self._h = C.c_void_p()
         if isinstance(num_qubits, QubitRegister):
             src = num_qubits
+            src._flush()
             check(lib.iqsg_clone(src._h, C.byref(self._h)))
             self._n, self._prec = src._n, src._prec
             self.qubit_permutation = src.qubit_permutation.copy()
@@ -91,6 +104,7 @@ class QubitRegister:
 
     def _init_flags(self):
         self.gate_counter: Optional[GateCounter] = None
+        self._queue = []
         self.fusion = False
         self.log2llc = 20
         self.specialize = False
@@ -246,8 +260,11 @@ class QubitRegister:
 
     # ---- fusion / specialisation toggles ----------------------------------------------------
     def TurnOnFusion(self, log2llc: int = 20) -> None:
-        """The reference replays buffered gates block by block with unchanged arithmetic
-        (src/qureg_fusion.cpp:12-94); results here are identical with fusion on or off."""
+        """Queue gates and apply them in fused sweeps (iqsg_apply_ops): each pass over the
+        state applies several gates in registers. The reference buffers gates below
+        position log2llc and replays them block by block (src/qureg_fusion.cpp:12-94);
+        here every gate is queued, whatever its position, and the queue is applied before
+        anything reads or reorders the state. Results equal the unfused ones."""
         self.fusion = True
         self.log2llc = int(log2llc)
 
@@ -258,8 +275,28 @@ class QubitRegister:
     def IsFusionEnabled(self) -> bool:
         return self.fusion
 
-    def ApplyFusedGates(self) -> None:
-        pass
+    def ApplyFusedGates(self) -> int:
+        """Apply the queued gates; returns the number of passes over the state it took."""
+        if not self._queue:
+            return 0
+        arr = (_lib.Op * len(self._queue))(*self._queue)
+        self._queue = []
+        sweeps = C.c_uint()
+        check(lib.iqsg_apply_ops(self._h, arr, len(arr), C.byref(sweeps)))
+        return sweeps.value
+
+    _flush = ApplyFusedGates
+
+    def SetSweepWidth(self, kmax: int) -> None:
+        """Largest number of target qubits one fused pass holds in registers (1..4, 0 =
+        default for the precision)."""
+        self._flush()
+        check(lib.iqsg_set_sweep_width(self._h, int(kmax)))
+
+    def _enqueue(self, op) -> None:
+        self._queue.append(op)
+        if len(self._queue) >= 4096:
+            self._flush()
 
     def TurnOnSpecialize(self) -> None:
         self.specialize = True
@@ -285,7 +322,10 @@ class QubitRegister:
         m8 = _m2(m)
         p = self._pos(qubit, "Apply1QubitGate")
         self._count1(qubit)
-        check(lib.iqsg_apply_1q(self._h, p, dptr(m8)))
+        if self.fusion:
+            self._enqueue(_op(_lib.OP_1Q, p, 0, m8))
+        else:
+            check(lib.iqsg_apply_1q(self._h, p, dptr(m8)))
 
     def ApplyControlled1QubitGate(self, control: int, target: int, m, spec=None, angle: float = 0.0) -> None:
         """src/qureg_applyctrl1qubitgate.cpp:414-444."""
@@ -294,7 +334,10 @@ class QubitRegister:
         if control == target:
             raise ValueError("ApplyControlled1QubitGate: control and target coincide")
         self._count2(control, target)
-        check(lib.iqsg_apply_controlled_1q(self._h, pc, pt, dptr(m8)))
+        if self.fusion:
+            self._enqueue(_op(_lib.OP_CTRL, pt, 0, m8, ctrl=(pc,)))
+        else:
+            check(lib.iqsg_apply_controlled_1q(self._h, pc, pt, dptr(m8)))
 
     def Apply2QubitGate(self, qubit_high: int, qubit_low: int, m) -> None:
         """src/qureg_apply2qubitgate.cpp:14-73."""
@@ -302,7 +345,10 @@ class QubitRegister:
         ph, pl = self._pos(qubit_high, "Apply2QubitGate"), self._pos(qubit_low, "Apply2QubitGate")
         if qubit_high == qubit_low:
             raise ValueError("Apply2QubitGate: qubits coincide")
-        check(lib.iqsg_apply_2q(self._h, ph, pl, dptr(m32)))
+        if self.fusion:
+            self._enqueue(_op(_lib.OP_2Q, ph, pl, m32))
+        else:
+            check(lib.iqsg_apply_2q(self._h, ph, pl, dptr(m32)))
         self._count2(qubit_high, qubit_low)
 
     def ApplyDiag(self, qubit_1: int, qubit_2: int, m) -> None:
@@ -315,7 +361,10 @@ class QubitRegister:
         if qubit_1 == qubit_2:
             raise ValueError("ApplyDiag: qubits coincide")
         self._count2(qubit_1, qubit_2)
-        check(lib.iqsg_apply_diag_2q(self._h, p1, p2, dptr(d)))
+        if self.fusion:
+            self._enqueue(_op(_lib.OP_DIAG2, p1, p2, d))
+        else:
+            check(lib.iqsg_apply_diag_2q(self._h, p1, p2, dptr(d)))
 
     ApplyDiagonalGate = ApplyDiag
 
@@ -324,6 +373,10 @@ class QubitRegister:
         m8 = _m2(m)
         check_distinct(list(controls) + [target], self._n, "ApplyMultiControlled1QubitGate")
         pc = np.asarray([self.qubit_permutation.map[c] for c in controls], dtype=np.uint32)
+        if self.fusion and len(pc) <= 4:
+            self._enqueue(_op(_lib.OP_CTRL, self.qubit_permutation.map[target], 0, m8, ctrl=[int(c) for c in pc]))
+            return
+        self._flush()
         check(lib.iqsg_apply_multi_controlled_1q(self._h, len(pc), uptr(pc), self.qubit_permutation.map[target],
                                                  dptr(m8)))
 
@@ -422,7 +475,10 @@ class QubitRegister:
         # it had to swap them (src/qureg_applyswap.cpp:140-144).
         if p1 > p2 and (m8[2] != m8[4] or m8[3] != m8[5]):
             raise ValueError(f"{what}: the 2x2 block must be symmetric (m01 == m10)")
-        check(lib.iqsg_apply_swaplike(self._h, p1, p2, dptr(m8)))
+        if self.fusion:
+            self._enqueue(_op(_lib.OP_SWAPLIKE, p1, p2, m8))
+        else:
+            check(lib.iqsg_apply_swaplike(self._h, p1, p2, dptr(m8)))
 
     def ApplySwap(self, qubit1: int, qubit2: int) -> None:
         """src/qureg_applyswap.cpp:23-29."""
@@ -458,7 +514,11 @@ class QubitRegister:
                 self.gate_counter.TwoQubitIncrement(a, b)
         pc = np.asarray([self.qubit_permutation.map[control_1], self.qubit_permutation.map[control_2]], dtype=np.uint32)
         m8 = _m2([[0, 1], [1, 0]])
-        check(lib.iqsg_apply_multi_controlled_1q(self._h, 2, uptr(pc), self.qubit_permutation.map[target], dptr(m8)))
+        if self.fusion:
+            self._enqueue(_op(_lib.OP_CTRL, self.qubit_permutation.map[target], 0, m8, ctrl=[int(c) for c in pc]))
+        else:
+            check(lib.iqsg_apply_multi_controlled_1q(self._h, 2, uptr(pc), self.qubit_permutation.map[target],
+                                                     dptr(m8)))
 
     # ---- permutation of the qubit order ---------------------------------------------------------------
     def PermuteQubits(self, new_map: Sequence[int], style_of_map: str = "direct") -> None:
@@ -612,3 +672,28 @@ class QubitRegister:
 
     def __repr__(self) -> str:
         return f"<QubitRegister {self._n} qubits {self.precision} on GPU>"
+
+
+def _flushing(fn):
+    """Apply queued (fused) gates of every register argument before fn reads or changes
+    the state outside the gate stream."""
+    import functools
+
+    @functools.wraps(fn)
+    def wrapper(self, *args, **kwargs):
+        if self._queue:
+            self._flush()
+        for a in args:
+            if isinstance(a, QubitRegister) and a._queue:
+                a._flush()
+        return fn(self, *args, **kwargs)
+    return wrapper
+
+
+for _name in ("SetMath", "RawState", "synchronize", "Initialize", "InitializationWithSameAmplitudeEverywhere",
+              "GetStateVector", "SetStateVector", "__getitem__", "__setitem__", "PermuteQubits", "GetProbability",
+              "CollapseQubit", "IsClassicalBit", "GetClassicalValue", "ExpectationValue", "ComputeNorm", "Normalize",
+              "ComputeOverlap", "MaxAbsDiff", "MaxL2NormDiff", "AmplitudeWiseScalarMultiplication",
+              "AmplitudeWiseSum", "__eq__"):
+    setattr(QubitRegister, _name, _flushing(getattr(QubitRegister, _name)))
+QubitRegister.PermuteLocalQubits = QubitRegister.PermuteQubits

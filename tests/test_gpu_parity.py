@@ -26,19 +26,20 @@ def _gpu_reg(iqs, n, prec, math_mode, style="base", base=0):
     return iqs.QubitRegister(n, style, base, precision=prec, math=math_mode)
 
 
+@pytest.mark.parametrize("fused", [False, True])
 @pytest.mark.parametrize("math_mode", ["native", "emulated"])
 @pytest.mark.parametrize("prefix", ["kat_", "random_", "collapse_", "fusion_", "plain_"])
-def test_golden_cases(iqs, golden, prefix, math_mode):
+def test_golden_cases(iqs, golden, prefix, math_mode, fused):
     for name in golden_cases(golden, prefix):
         meta = case_meta(golden, name)
         prec = meta["precision"]
         reg = _gpu_reg(iqs, meta["n"], prec, math_mode, meta["style"], meta["base"])
         if f"{name}/init" in golden:
             reg.SetStateVector(golden[f"{name}/init"])
-        if meta.get("fusion") is not None:
-            reg.TurnOnFusion(meta["fusion"])
+        if fused or meta.get("fusion") is not None:
+            reg.TurnOnFusion(meta.get("fusion") or 20)
         q = np.asarray(replay(reg, case_ops(golden, name)))
-        if meta.get("fusion") is not None:
+        if fused or meta.get("fusion") is not None:
             reg.TurnOffFusion()
         tol = TOL_DP if prec == "DP" else TOL_SP
         err = compare_final(golden, name, reg.GetStateVector().astype(np.complex128), tol)
@@ -85,6 +86,47 @@ def test_random_circuits_vs_oracle(iqs, n, seed, prec, math_mode):
     assert np.max(np.abs(a.GetStateVector() - b.GetStateVector())) <= tol
     assert a.perm.map == b.qubit_permutation.map
     assert np.max(np.abs(qa - qb), initial=0.0) <= tol
+
+
+@pytest.mark.parametrize("prec,math_mode", MODES)
+@pytest.mark.parametrize("width", [1, 2, 3, 4])
+@pytest.mark.parametrize("n,seed,nops", [(6, 601, 300), (13, 602, 300), (18, 603, 120)])
+def test_fused_sweeps_vs_oracle(iqs, n, seed, nops, width, prec, math_mode):
+    """Fused sweeps of every width over mixed circuits (1q, controlled, 2q dense, swap family,
+    diagonal, Toffoli) against the oracle applying the same gates one by one. From 16 qubits
+    up the sweeps run in the bulk-copy pipelined kernel."""
+    rng = np.random.default_rng(seed)
+    init = random_state(n, rng)
+    ops = random_circuit(n, nops, rng, permutes=True, queries=True)
+    a = oracle.OracleRegister(n, "base", 0, prec)
+    a.SetStateVector(init)
+    b = _gpu_reg(iqs, n, prec, math_mode)
+    b.SetStateVector(init)
+    b.SetSweepWidth(width)
+    b.TurnOnFusion()
+    qa, qb = np.asarray(replay(a, ops)), np.asarray(replay(b, ops))
+    b.TurnOffFusion()
+    tol = TOL_DP if prec == "DP" else TOL_SP
+    assert np.max(np.abs(a.GetStateVector() - b.GetStateVector())) <= tol
+    assert np.max(np.abs(qa - qb), initial=0.0) <= tol
+
+
+def test_fused_native_is_bit_identical_to_unfused(iqs):
+    """In native FP64 a fused sweep performs the same operations as the per-gate kernels."""
+    n = 12
+    rng = np.random.default_rng(701)
+    init = random_state(n, rng)
+    ops = brick_layer_ops(n, rng, "ApplyCPauliZ") + brick_layer_ops(n, rng, "ApplyCPauliX")
+    a = iqs.QubitRegister(n, "base", 0)
+    b = iqs.QubitRegister(n, "base", 0)
+    a.SetStateVector(init)
+    b.SetStateVector(init)
+    replay(a, ops)
+    b.TurnOnFusion()
+    replay(b, ops)
+    sweeps = b.ApplyFusedGates()
+    assert 0 < sweeps < len(ops)
+    assert np.array_equal(a.GetStateVector(), b.GetStateVector())
 
 
 @pytest.mark.parametrize("prec,math_mode", MODES)
