@@ -238,6 +238,29 @@ int iqsg_cost_expectation(iqsg_state* psi, const iqsg_state* diag, int power, do
  * InitializeVectorAsMaxCutCostFunction: src/qaoa_features.cpp:73-143. */
 int iqsg_maxcut_cost(iqsg_state* diag, const int* adj, const unsigned* map, int* max_cut);
 
+/* ---- QAOA MaxCut circuits and adjoint gradients ---------------------------------------- */
+
+/* One QAOA layer: amp *= exp(-i gamma H_C) with H_C = 1/2 sum_e w_e Z_u Z_v, then
+ * exp(-i beta X_q) (= RX(2 beta)) on every qubit. edges: 2*num_edges data positions
+ * (u0, v0, u1, v1, ...); weights: num_edges ints in [0, 255] or NULL for unit weights.
+ * The cost phase equals qaoa::ImplementQaoaLayerBasedOnCostFunction with the MaxCut cost
+ * vector (src/qaoa_features.cpp:248-264) up to a global phase; the mixer equals
+ * ApplyRotationX(q, 2 beta) on every qubit (src/qureg_apply1qubitgate.cpp:277-283). */
+int iqsg_qaoa_layer(iqsg_state* h, unsigned num_edges, const unsigned* edges, const int* weights, double gamma,
+                    double beta);
+
+/* energy = <psi|O|psi> with O = sum_e w_e Z_u Z_v (= sum of ExpectationValueZZ over edges,
+ * src/qureg_expectval.cpp:365-375), *norm2 = <psi|psi> (may be NULL). With lam != NULL also
+ * writes lam = O psi, the starting adjoint state of a gradient. */
+int iqsg_qaoa_observable(iqsg_state* psi, iqsg_state* lam, unsigned num_edges, const unsigned* edges,
+                         const int* weights, double* energy, double* norm2);
+
+/* Adjoint step back through one layer: with psi and lam taken after the layer, returns
+ * dE/dgamma and dE/dbeta of that layer and leaves psi, lam undone to before it.
+ * No counterpart in the reference (it has no gradients). */
+int iqsg_qaoa_layer_backward(iqsg_state* psi, iqsg_state* lam, unsigned num_edges, const unsigned* edges,
+                             const int* weights, double gamma, double beta, double* grad_gamma, double* grad_beta);
+
 /* ---- allocation-free measurement -------------------------------------------------------- */
 
 /* Probability of |1> on position pos (sum of |amp|^2 over indices with that bit set) for

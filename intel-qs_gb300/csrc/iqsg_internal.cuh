@@ -31,9 +31,12 @@ constexpr int kThreads = 256;
 constexpr int kMaxPartials = 4096;
 // scratch layout (doubles): [0, 2*kMaxPartials) partials, then 8 result slots.
 constexpr int kResultSlot = 2 * kMaxPartials;
-constexpr int kScratchDoubles = 2 * kMaxPartials + 16;
 // scratch[kErrorSlot] (as unsigned long long): set by a kernel whose bounded wait ran out.
 constexpr int kErrorSlot = 2 * kMaxPartials + 8;
+// scratch[kTableSlot ...]: small per-call tables (QAOA phases: 2 doubles per cut value).
+constexpr int kTableSlot = 2 * kMaxPartials + 16;
+constexpr int kTableDoubles = 2 * 1040;
+constexpr int kScratchDoubles = kTableSlot + kTableDoubles;
 // Registers from this size up use the bulk-copy pipelined sweep kernels.
 constexpr unsigned kBulkMinQubits = 16;
 

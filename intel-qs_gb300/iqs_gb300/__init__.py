@@ -11,6 +11,7 @@ All state lives in GPU memory; every operation runs as a CUDA kernel in libiqsg.
 from ._lib import IqsgError, LIB_PATH, lib
 from .permutation import GateCounter, Permutation
 from .qureg import QubitRegister
+from .adjoint import QaoaMaxCut, qaoa_energy
 from .qaoa import (GetExpectationValueFromCostFunction, GetExpectationValueSquaredFromCostFunction,
                    ImplementQaoaLayerBasedOnCostFunction, InitializeVectorAsMaxCutCostFunction)
 
@@ -18,4 +19,5 @@ __all__ = [
     "QubitRegister", "Permutation", "GateCounter", "IqsgError", "LIB_PATH", "lib",
     "InitializeVectorAsMaxCutCostFunction", "ImplementQaoaLayerBasedOnCostFunction",
     "GetExpectationValueFromCostFunction", "GetExpectationValueSquaredFromCostFunction",
+    "QaoaMaxCut", "qaoa_energy",
 ]

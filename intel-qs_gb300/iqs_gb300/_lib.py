@@ -74,6 +74,9 @@ SIGNATURES = {
     "iqsg_maxcut_cost": [_P, _IP, _UP, _IP],
     "iqsg_apply_ops": [_P, C.POINTER(Op), _U, _UP],
     "iqsg_set_sweep_width": [_P, _U],
+    "iqsg_qaoa_layer": [_P, _U, _UP, _IP, _D, _D],
+    "iqsg_qaoa_observable": [_P, _P, _U, _UP, _IP, _DP, _DP],
+    "iqsg_qaoa_layer_backward": [_P, _P, _U, _UP, _IP, _D, _D, _DP, _DP],
     "iqsg_probability_static": [_P, _U, C.c_int, _U, _P, _P],
 }
 _RESTYPES = {"iqsg_last_error": C.c_char_p}

@@ -1,0 +1,15 @@
+"""The C++ drop-in header compiles on a machine without a GPU (syntax and templates only)."""
+import subprocess
+
+from conftest import REPO
+
+
+def test_cpp_header_compiles(tmp_path):
+    src = tmp_path / "t.cpp"
+    src.write_text('#include "iqs_gb300/qureg.hpp"\n'
+                   "template class iqs::QubitRegister<ComplexDP>;\n"
+                   "template class iqs::QubitRegister<ComplexSP>;\n"
+                   "int main() { return 0; }\n")
+    subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(REPO / "include"), str(src)], check=True)
+    subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(REPO / "include"),
+                    str(REPO / "tests" / "cpp" / "shim_driver.cpp")], check=True)
