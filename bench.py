@@ -177,6 +177,68 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def regular_graph(n: int, degree: int, seed: int) -> list:
+    """Seeded random regular graph: configuration model, redrawn until simple."""
+    rng = np.random.default_rng(seed)
+    while True:
+        stubs = rng.permutation(np.repeat(np.arange(n), degree))
+        pairs = stubs.reshape(-1, 2)
+        edges = {tuple(sorted((int(a), int(b)))) for a, b in pairs}
+        if all(a != b for a, b in edges) and len(edges) == len(pairs):
+            return sorted(edges)
+
+
+def qaoa_section(n: int = 26, p: int = 8, stream=None) -> dict:
+    """QAOA MaxCut on a 3-regular graph: adjoint gradient vs central finite differences on
+    the GPU (same forward kernels; h = 1e-6), and vs finite differences through the plain
+    per-gate public API (cost vector + one RX kernel per qubit), ComplexDP."""
+    import iqs_gb300 as iqs
+    import torch
+    edges = regular_graph(n, 3, seed=3)
+    rng = np.random.default_rng(4)
+    gammas, betas = rng.uniform(0, np.pi, p), rng.uniform(0, np.pi, p)
+    circ = iqs.QaoaMaxCut(n, edges, stream=stream)
+    circ.energy_and_grad(gammas, betas)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e, dg, db = circ.energy_and_grad(gammas, betas)
+    t_adj = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    fdg, fdb = circ.finite_difference_grad(gammas, betas, h=1e-6)
+    t_fd = time.perf_counter() - t0
+    g, fd = np.concatenate([dg, db]), np.concatenate([fdg, fdb])
+    rel = float(np.max(np.abs(g - fd)) / np.max(np.abs(fd)))
+    # One energy through the plain per-gate API, then 2P of them for the plain FD figure.
+    adj = np.zeros((n, n), dtype=np.int32)
+    for u, v in edges:
+        adj[u, v] = adj[v, u] = 1
+    diag = iqs.QubitRegister(n, "base", 0, stream=stream)
+    iqs.InitializeVectorAsMaxCutCostFunction(diag, adj.reshape(-1))
+    psi = iqs.QubitRegister(n, "++++", 0, stream=stream)
+
+    def plain_energy():
+        psi.Initialize("++++", 0)
+        for gm, bt in zip(gammas, betas):
+            iqs.ImplementQaoaLayerBasedOnCostFunction(psi, diag, -gm)
+            for q in range(n):
+                psi.ApplyRotationX(q, 2 * bt)
+        return len(edges) - 2 * iqs.GetExpectationValueFromCostFunction(psi, diag)
+
+    e_plain = plain_energy()
+    t0 = time.perf_counter()
+    plain_energy()
+    t_plain = (time.perf_counter() - t0) * 2 * 2 * p
+    del circ, diag, psi
+    return {"workload": f"QAOA MaxCut, random 3-regular graph on {n} vertices ({len(edges)} edges), p={p}, "
+                        f"16 parameters U[0, pi), ComplexDP, native FP64",
+            "energy": e, "energy_plain_api": e_plain,
+            "adjoint_s": round(t_adj, 4), "adjoint_grads_per_s": round(1 / t_adj, 3),
+            "fd_same_kernels_s": round(t_fd, 3), "fd_same_kernels_grads_per_s": round(1 / t_fd, 4),
+            "speedup_vs_fd_same_kernels": round(t_fd / t_adj, 2),
+            "fd_plain_api_s": round(t_plain, 3), "speedup_vs_fd_plain_api": round(t_plain / t_adj, 2),
+            "max_rel_diff_adjoint_vs_fd": rel}
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -205,8 +267,13 @@ def run_ours(args) -> None:
     reg = iqs.QubitRegister(n, "base", 0, math=args.math, stream=stream.cuda_stream)
     for q in range(n):  # a dense state: every amplitude nonzero
         reg.ApplyHadamard(q)
+    tuned = None
     if args.width:
         reg.SetSweepWidth(args.width)
+        reg.SetSweepPipeline(args.pipeline)
+    elif args.fusion:
+        from iqs_gb300.autotune import tune_fusion
+        tuned = tune_fusion(reg)  # untimed: picks the pass width and kernel for this register
     if args.fusion:
         reg.TurnOnFusion()
     total = args.warmup + args.steps
@@ -304,6 +371,7 @@ def run_ours(args) -> None:
     # Parity of the timed arithmetic on the same layer shape at 20 qubits vs the oracle.
     parity = None
     cpu = None
+    qaoa = None
     if rank == 0:
         import oracle
         oracle.build(ref=False)
@@ -322,6 +390,7 @@ def run_ours(args) -> None:
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             cpu = cpu_layer_gbs(args.cpu_qubits, 1, seed=5, threads=threads)
+        qaoa = None if args.no_adjoint else qaoa_section(stream=stream.cuda_stream)
 
     if rank == 0:
         dtype = "c128: f64 storage, double-float (fp32x2) products and sums" if args.math == "emulated" else "f64"
@@ -332,7 +401,10 @@ def run_ours(args) -> None:
             "data": "synthetic (seeded Haar-random gates on a dense state)",
             "config": {"workload": f"gate layer: Haar U on each of {n} qubits + CZ brick (15 even + 14 odd), ComplexDP",
                        "qubits": n, "state_bytes": (1 << n) * 16, "bytes_per_step": layer_bytes(n),
-                       "math": args.math, "fusion": bool(args.fusion), "sweep_width": args.width or "default",
+                       "math": args.math, "fusion": bool(args.fusion),
+                       "sweep_width": args.width or (tuned["width"] if tuned else "default"),
+                       "sweep_pipeline": bool(args.pipeline if args.width else (tuned["pipeline"] if tuned else False)),
+                       "autotune_ms": [[r["width"], r["pipeline"], round(r["ms"], 1)] for r in tuned["table"]] if tuned else None,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "state (16 GiB) far larger than L2 (129 MB); no flush needed"},
             "roofline": {"bound": "hbm", "kernel": kname,
@@ -348,6 +420,8 @@ def run_ours(args) -> None:
             "parity": {"max_abs_err_vs_oracle": parity, "case": "same layer shape at 20 qubits, 2 layers"},
         }
         line.update(other)
+        if qaoa is not None:
+            line["adjoint"] = qaoa
         if cpu is not None:
             line["cpu_baseline"] = {"value": round(cpu["gbs"], 3), "unit": UNIT, "cores": cpu["cores"],
                                     "kind": cpu["kind"],
@@ -370,8 +444,11 @@ def main() -> None:
     ap.add_argument("--compare-native", action="store_true", default=True)
     ap.add_argument("--no-fusion", dest="fusion", action="store_false", default=True,
                     help="apply the layer gate by gate (one kernel per gate)")
-    ap.add_argument("--width", type=int, default=0, help="fused-pass width (target qubits per pass; 0 = default)")
+    ap.add_argument("--width", type=int, default=0,
+                    help="fused-pass width (target qubits per pass); 0 = chosen by the autotuner")
+    ap.add_argument("--pipeline", type=int, default=0, help="with --width: 1 = bulk-copy pipelined passes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the QAOA adjoint-gradient section")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per 1-qubit-gate launch from an ncu capture, if known")
     args = ap.parse_args()

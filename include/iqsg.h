@@ -201,6 +201,17 @@ int iqsg_apply_ops(iqsg_state* h, const iqsg_op* ops, unsigned count, unsigned* 
  * src/qureg_fusion.cpp:12-31. */
 int iqsg_set_sweep_width(iqsg_state* h, unsigned kmax);
 
+/* Tuning options of a register (iqsg_set_option). */
+typedef enum {
+  IQSG_OPT_SWEEP_WIDTH = 0,    /* same as iqsg_set_sweep_width */
+  IQSG_OPT_SWEEP_PIPELINE = 1  /* 1: fused passes on registers of 16+ qubits stream tiles through
+                                  shared memory with bulk async copies; 0 (default): each thread
+                                  loads its groups directly */
+} iqsg_option;
+
+/* Set a tuning option; results never depend on it. */
+int iqsg_set_option(iqsg_state* h, int option, int value);
+
 /* ---- reductions (FP64 accumulation; each waits for its result) ------------------------ */
 
 /* Sum of |amp|^2 over indices with bit pos = 1. Replaces GetProbability:

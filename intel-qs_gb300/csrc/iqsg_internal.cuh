@@ -21,7 +21,7 @@ struct iqsg_state {
   void* tmp = nullptr;            // device: out-of-place permutation buffer (lazy)
   size_t tmp_bytes = 0;
   unsigned sweep_width = 0;       // fused-sweep width limit (0 = default for the precision)
-  bool no_bulk = false;           // force the non-pipelined sweep kernels (comparison / tests)
+  bool bulk = false;              // fused passes through the bulk-copy pipeline (IQSG_OPT_SWEEP_PIPELINE)
 };
 
 namespace iqsg {

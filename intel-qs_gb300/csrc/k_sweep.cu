@@ -330,7 +330,7 @@ void launch_k(iqsg_state* h, const SweepParams& P) {
   const uint64_t ngroups = h->N >> K;
   const bool df = h->prec == IQSG_COMPLEX_DP && h->math == IQSG_MATH_EMULATED && K <= 3;
   TileGeom g;
-  if (h->n >= kBulkMinQubits && !h->no_bulk && make_geometry(P, h->n, g)) {
+  if (h->bulk && h->n >= kBulkMinQubits && make_geometry(P, h->n, g)) {
     if (h->prec == IQSG_COMPLEX_SP) launch_bulk<float, false, K>(h, P, g);
     else if (df) launch_bulk<double, (K <= 3), K>(h, P, g);
     else launch_bulk<double, false, K>(h, P, g);
@@ -575,6 +575,19 @@ extern "C" int iqsg_set_sweep_width(iqsg_state* h, unsigned kmax) {
   if (kmax > (unsigned)kSweepMaxK) return fail(IQSG_EINVAL, "iqsg_set_sweep_width: width %u above %d", kmax, kSweepMaxK);
   h->sweep_width = kmax;
   return IQSG_OK;
+}
+
+extern "C" int iqsg_set_option(iqsg_state* h, int option, int value) {
+  if (!h) return fail(IQSG_EINVAL, "null register handle");
+  switch (option) {
+    case IQSG_OPT_SWEEP_WIDTH:
+      return iqsg_set_sweep_width(h, (unsigned)value);
+    case IQSG_OPT_SWEEP_PIPELINE:
+      h->bulk = value != 0;
+      return IQSG_OK;
+    default:
+      return fail(IQSG_EINVAL, "iqsg_set_option: unknown option %d", option);
+  }
 }
 
 extern "C" int iqsg_apply_ops(iqsg_state* h, const iqsg_op* ops, unsigned count, unsigned* sweeps) {

@@ -15,6 +15,7 @@ LIB_PATH = _HERE / "libiqsg.so"
 IQSG_OK, IQSG_EINVAL, IQSG_ENOMEM, IQSG_EDEVICE, IQSG_ETIMEOUT, IQSG_ENOTSUP = range(6)
 COMPLEX_DP, COMPLEX_SP = 0, 1
 MATH_NATIVE, MATH_EMULATED = 0, 1
+OPT_SWEEP_WIDTH, OPT_SWEEP_PIPELINE = 0, 1
 
 _P = C.c_void_p
 _U = C.c_uint
@@ -74,6 +75,7 @@ SIGNATURES = {
     "iqsg_maxcut_cost": [_P, _IP, _UP, _IP],
     "iqsg_apply_ops": [_P, C.POINTER(Op), _U, _UP],
     "iqsg_set_sweep_width": [_P, _U],
+    "iqsg_set_option": [_P, C.c_int, C.c_int],
     "iqsg_qaoa_layer": [_P, _U, _UP, _IP, _D, _D],
     "iqsg_qaoa_observable": [_P, _P, _U, _UP, _IP, _DP, _DP],
     "iqsg_qaoa_layer_backward": [_P, _P, _U, _UP, _IP, _D, _D, _DP, _DP],

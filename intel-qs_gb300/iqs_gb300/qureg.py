@@ -293,6 +293,12 @@ class QubitRegister:
         self._flush()
         check(lib.iqsg_set_sweep_width(self._h, int(kmax)))
 
+    def SetSweepPipeline(self, on: bool) -> None:
+        """Stream fused passes through shared memory with bulk async copies (registers of 16+
+        qubits); a tuning choice that never changes results."""
+        self._flush()
+        check(lib.iqsg_set_option(self._h, _lib.OPT_SWEEP_PIPELINE, 1 if on else 0))
+
     def _enqueue(self, op) -> None:
         self._queue.append(op)
         if len(self._queue) >= 4096:

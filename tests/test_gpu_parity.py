@@ -90,11 +90,12 @@ def test_random_circuits_vs_oracle(iqs, n, seed, prec, math_mode):
 
 @pytest.mark.parametrize("prec,math_mode", MODES)
 @pytest.mark.parametrize("width", [1, 2, 3, 4])
-@pytest.mark.parametrize("n,seed,nops", [(6, 601, 300), (13, 602, 300), (18, 603, 120)])
-def test_fused_sweeps_vs_oracle(iqs, n, seed, nops, width, prec, math_mode):
+@pytest.mark.parametrize("n,seed,nops,pipeline", [(6, 601, 300, False), (13, 602, 300, False),
+                                                  (18, 603, 120, False), (18, 604, 120, True)])
+def test_fused_sweeps_vs_oracle(iqs, n, seed, nops, pipeline, width, prec, math_mode):
     """Fused sweeps of every width over mixed circuits (1q, controlled, 2q dense, swap family,
-    diagonal, Toffoli) against the oracle applying the same gates one by one. From 16 qubits
-    up the sweeps run in the bulk-copy pipelined kernel."""
+    diagonal, Toffoli) against the oracle applying the same gates one by one, with the direct
+    and (from 16 qubits) the bulk-copy pipelined kernels."""
     rng = np.random.default_rng(seed)
     init = random_state(n, rng)
     ops = random_circuit(n, nops, rng, permutes=True, queries=True)
@@ -103,6 +104,7 @@ def test_fused_sweeps_vs_oracle(iqs, n, seed, nops, width, prec, math_mode):
     b = _gpu_reg(iqs, n, prec, math_mode)
     b.SetStateVector(init)
     b.SetSweepWidth(width)
+    b.SetSweepPipeline(pipeline)
     b.TurnOnFusion()
     qa, qb = np.asarray(replay(a, ops)), np.asarray(replay(b, ops))
     b.TurnOffFusion()
