@@ -197,7 +197,7 @@ def qaoa_section(n: int = 26, p: int = 8, stream=None) -> dict:
     edges = regular_graph(n, 3, seed=3)
     rng = np.random.default_rng(4)
     gammas, betas = rng.uniform(0, np.pi, p), rng.uniform(0, np.pi, p)
-    circ = iqs.QaoaMaxCut(n, edges, stream=stream)
+    circ = iqs.QaoaMaxCut(n, edges, stream=stream, checkpoint=True)
     circ.energy_and_grad(gammas, betas)  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -230,7 +230,7 @@ def qaoa_section(n: int = 26, p: int = 8, stream=None) -> dict:
     t_plain = (time.perf_counter() - t0) * 2 * 2 * p
     del circ, diag, psi
     return {"workload": f"QAOA MaxCut, random 3-regular graph on {n} vertices ({len(edges)} edges), p={p}, "
-                        f"16 parameters U[0, pi), ComplexDP, native FP64",
+                        f"16 parameters U[0, pi), ComplexDP, native FP64, checkpointed adjoint (2p saved states)",
             "energy": e, "energy_plain_api": e_plain,
             "adjoint_s": round(t_adj, 4), "adjoint_grads_per_s": round(1 / t_adj, 3),
             "fd_same_kernels_s": round(t_fd, 3), "fd_same_kernels_grads_per_s": round(1 / t_fd, 4),

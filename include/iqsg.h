@@ -272,6 +272,18 @@ int iqsg_qaoa_observable(iqsg_state* psi, iqsg_state* lam, unsigned num_edges, c
 int iqsg_qaoa_layer_backward(iqsg_state* psi, iqsg_state* lam, unsigned num_edges, const unsigned* edges,
                              const int* weights, double gamma, double beta, double* grad_gamma, double* grad_beta);
 
+/* Checkpointed layer: as iqsg_qaoa_layer, and after_cost / after_mixer (registers of the same
+ * size) receive the state after the cost phase and after the whole layer. */
+int iqsg_qaoa_layer_ckpt(iqsg_state* h, iqsg_state* after_cost, iqsg_state* after_mixer, unsigned num_edges,
+                         const unsigned* edges, const int* weights, double gamma, double beta);
+
+/* Adjoint step from checkpoints: only lam is walked back through the layer; the two
+ * checkpoints of that layer are read. Returns the layer's dE/dgamma and dE/dbeta.
+ * No counterpart in the reference. */
+int iqsg_qaoa_layer_backward_ckpt(iqsg_state* lam, const iqsg_state* after_cost, const iqsg_state* after_mixer,
+                                  unsigned num_edges, const unsigned* edges, const int* weights, double gamma,
+                                  double beta, double* grad_gamma, double* grad_beta);
+
 /* ---- allocation-free measurement -------------------------------------------------------- */
 
 /* Probability of |1> on position pos (sum of |amp|^2 over indices with that bit set) for

@@ -40,6 +40,8 @@ struct LayerParams {
   double c, s;           // cos(beta), sin(beta) of exp(-i beta X) (s negated to undo it)
   int cost_pre;          // forward: apply the cost phase before the rotations
   int cost_post;         // backward: accumulate the H_C term and undo the cost phase after them
+  int xterms;            // checkpointed backward: accumulate the X_q terms (lambda not yet walked back)
+  int rotate;            // checkpointed backward: undo the rotations on lambda and store it
   unsigned W;
   double half_w;         // W / 2
 };
@@ -81,8 +83,10 @@ __device__ __forceinline__ void group_index(const LayerParams& L, uint64_t g, ui
 }
 
 // Forward pass: optional cost phase, then exp(-i beta X_q) on the K active positions.
+// src may differ from psi (the first pass of a checkpointed layer reads the checkpoint).
 template <typename R, int K>
-__global__ void __launch_bounds__(kThreads) k_qaoa_fwd(typename V2<R>::type* __restrict__ psi, uint64_t ngroups,
+__global__ void __launch_bounds__(kThreads) k_qaoa_fwd(typename V2<R>::type* __restrict__ psi,
+                                                       const typename V2<R>::type* __restrict__ src, uint64_t ngroups,
                                                        const __grid_constant__ LayerParams L,
                                                        const __grid_constant__ Graph G,
                                                        const double2* __restrict__ table) {
@@ -94,7 +98,7 @@ __global__ void __launch_bounds__(kThreads) k_qaoa_fwd(typename V2<R>::type* __r
     CX<R> a[Gs];
 #pragma unroll
     for (int k = 0; k < Gs; ++k) {
-      const auto v = psi[idx[k]];
+      const auto v = src[idx[k]];
       a[k].re = v.x;
       a[k].im = v.y;
     }
@@ -224,6 +228,94 @@ __global__ void __launch_bounds__(kThreads) k_qaoa_bwd(typename V2<R>::type* __r
   }
 }
 
+// dst = exp(-i gamma H_C) src (the after-cost checkpoint of a layer).
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_qaoa_cost_to(const typename V2<R>::type* __restrict__ src,
+                                                           typename V2<R>::type* __restrict__ dst, uint64_t N,
+                                                           const __grid_constant__ Graph G,
+                                                           const double2* __restrict__ table) {
+  for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < N; x += (uint64_t)gridDim.x * blockDim.x) {
+    const auto v = src[x];
+    const double2 ph = table[cut_of(x, G)];
+    typename V2<R>::type o;
+    cmul_fma<R>((R)ph.x, (R)ph.y, v.x, v.y, o.x, o.y);
+    dst[x] = o;
+  }
+}
+
+// Backward pass from checkpoints: psi after the mixer (pm) and after the cost phase (pc) are
+// read, never changed; only lambda is walked back. The X_q terms pair lambda with pm, so they
+// are taken in a first set of passes (xterms) before any rotation of the layer is undone on
+// lambda; the rotate passes then undo the rotations and, on the last one, take the H_C term
+// against pc and undo the cost phase.
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_qaoa_bwd_ckpt(const typename V2<R>::type* __restrict__ pm,
+                                                            const typename V2<R>::type* __restrict__ pc,
+                                                            typename V2<R>::type* __restrict__ lam, uint64_t ngroups,
+                                                            const __grid_constant__ LayerParams L,
+                                                            const __grid_constant__ Graph G,
+                                                            const double2* __restrict__ table,
+                                                            double* __restrict__ partials) {
+  constexpr int Gs = 1 << K;
+  const R c = (R)L.c, s = (R)L.s;
+  double gb = 0.0, gg = 0.0;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t idx[Gs];
+    group_index<K>(L, g, idx);
+    CX<R> l[Gs];
+#pragma unroll
+    for (int k = 0; k < Gs; ++k) {
+      const auto w = lam[idx[k]];
+      l[k].re = w.x;
+      l[k].im = w.y;
+    }
+    if (L.xterms) {
+#pragma unroll
+      for (int j = 0; j < K; ++j)
+#pragma unroll
+        for (int k = 0; k < Gs; ++k)
+          if (!(k & (1 << j))) {
+            const int k1 = k | (1 << j);
+            const auto p0 = pm[idx[k]], p1 = pm[idx[k1]];
+            gb += (double)l[k].re * (double)p1.y - (double)l[k].im * (double)p1.x +
+                  (double)l[k1].re * (double)p0.y - (double)l[k1].im * (double)p0.x;
+          }
+    }
+    if (!L.rotate) continue;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+#pragma unroll
+      for (int k = 0; k < Gs; ++k)
+        if (!(k & (1 << j))) rx_pair(c, s, l[k], l[k | (1 << j)]);
+    if (L.cost_post) {
+#pragma unroll
+      for (int k = 0; k < Gs; ++k) {
+        const unsigned cut = cut_of(idx[k], G);
+        const double gx = L.half_w - (double)cut;
+        const auto p = pc[idx[k]];
+        gg += gx * ((double)l[k].re * (double)p.y - (double)l[k].im * (double)p.x);
+        const double2 ph = table[cut];
+        CX<R> o;
+        cmul_fma<R>((R)ph.x, (R)ph.y, l[k].re, l[k].im, o.re, o.im);
+        l[k] = o;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < Gs; ++k) {
+      typename V2<R>::type v;
+      v.x = l[k].re;
+      v.y = l[k].im;
+      lam[idx[k]] = v;
+    }
+  }
+  double out[2];
+  block_sum2(gb, gg, out);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = out[0];
+    partials[kMaxPartials + blockIdx.x] = out[1];
+  }
+}
+
 // lambda = o(x) psi with o = W - 2 cut; energy partials sum o |psi|^2.
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_qaoa_observable(const typename V2<R>::type* __restrict__ psi,
@@ -311,10 +403,22 @@ void layer_positions(unsigned n, unsigned first, unsigned K, LayerParams& L) {
 }
 
 template <typename R, int K>
-void launch_fwd(iqsg_state* h, const LayerParams& L, const Graph& G, const double2* table) {
+void launch_fwd(iqsg_state* h, const void* src, const LayerParams& L, const Graph& G, const double2* table) {
   const uint64_t ng = h->N >> K;
-  k_qaoa_fwd<R, K><<<grid_for(ng, 1), kThreads, 0, h->stream>>>(reinterpret_cast<typename V2<R>::type*>(h->amps), ng,
-                                                                  L, G, table);
+  using V = typename V2<R>::type;
+  k_qaoa_fwd<R, K><<<grid_for(ng, 1), kThreads, 0, h->stream>>>(reinterpret_cast<V*>(h->amps),
+                                                                  reinterpret_cast<const V*>(src), ng, L, G, table);
+}
+
+template <typename R, int K>
+void launch_bwd_ckpt(iqsg_state* lam, const void* pm, const void* pc, const LayerParams& L, const Graph& G,
+                     const double2* table, unsigned grid) {
+  const uint64_t ng = lam->N >> K;
+  using V = typename V2<R>::type;
+  k_qaoa_bwd_ckpt<R, K><<<grid, kThreads, 0, lam->stream>>>(reinterpret_cast<const V*>(pm),
+                                                             reinterpret_cast<const V*>(pc),
+                                                             reinterpret_cast<V*>(lam->amps), ng, L, G, table,
+                                                             lam->scratch);
 }
 
 template <typename R, int K>
@@ -327,11 +431,21 @@ void launch_bwd(iqsg_state* h, iqsg_state* lam, const LayerParams& L, const Grap
 }
 
 template <typename R>
-void dispatch_fwd(iqsg_state* h, const LayerParams& L, const Graph& G, const double2* table) {
+void dispatch_fwd(iqsg_state* h, const void* src, const LayerParams& L, const Graph& G, const double2* table) {
   switch (L.K) {
-    case 1: launch_fwd<R, 1>(h, L, G, table); break;
-    case 2: launch_fwd<R, 2>(h, L, G, table); break;
-    case 3: launch_fwd<R, 3>(h, L, G, table); break;
+    case 1: launch_fwd<R, 1>(h, src, L, G, table); break;
+    case 2: launch_fwd<R, 2>(h, src, L, G, table); break;
+    case 3: launch_fwd<R, 3>(h, src, L, G, table); break;
+  }
+}
+
+template <typename R>
+void dispatch_bwd_ckpt(iqsg_state* lam, const void* pm, const void* pc, const LayerParams& L, const Graph& G,
+                       const double2* table, unsigned grid) {
+  switch (L.K) {
+    case 1: launch_bwd_ckpt<R, 1>(lam, pm, pc, L, G, table, grid); break;
+    case 2: launch_bwd_ckpt<R, 2>(lam, pm, pc, L, G, table, grid); break;
+    case 3: launch_bwd_ckpt<R, 3>(lam, pm, pc, L, G, table, grid); break;
   }
 }
 
@@ -383,8 +497,8 @@ extern "C" int iqsg_qaoa_layer(iqsg_state* h, unsigned num_edges, const unsigned
     L.cost_pre = first == 0;
     L.W = W;
     L.half_w = 0.5 * W;
-    if (h->prec == IQSG_COMPLEX_DP) dispatch_fwd<double>(h, L, G, table);
-    else dispatch_fwd<float>(h, L, G, table);
+    if (h->prec == IQSG_COMPLEX_DP) dispatch_fwd<double>(h, h->amps, L, G, table);
+    else dispatch_fwd<float>(h, h->amps, L, G, table);
   }
   return cuda_status(cudaGetLastError(), "iqsg_qaoa_layer");
 }
@@ -449,6 +563,98 @@ extern "C" int iqsg_qaoa_layer_backward(iqsg_state* psi, iqsg_state* lam, unsign
     if ((st = read2(psi, out, "iqsg_qaoa_layer_backward"))) return st;
     gb += out[0];
     gg += out[1];
+  }
+  *grad_beta = 2.0 * gb;
+  *grad_gamma = 2.0 * gg;
+  return IQSG_OK;
+}
+
+namespace {
+int check_same(const iqsg_state* a, const iqsg_state* b, const char* what) {
+  if (!a || !b) return fail(IQSG_EINVAL, "%s: null register", what);
+  if (a->n != b->n || a->prec != b->prec) return fail(IQSG_EINVAL, "%s: registers differ in size or precision", what);
+  return IQSG_OK;
+}
+}  // namespace
+
+extern "C" int iqsg_qaoa_layer_ckpt(iqsg_state* h, iqsg_state* after_cost, iqsg_state* after_mixer, unsigned num_edges,
+                                    const unsigned* edges, const int* weights, double gamma, double beta) {
+  int st = check_same(h, after_cost, "iqsg_qaoa_layer_ckpt");
+  if (!st) st = check_same(h, after_mixer, "iqsg_qaoa_layer_ckpt");
+  if (st) return st;
+  for (iqsg_state* o : {after_cost, after_mixer})
+    if (o->stream != h->stream) cudaStreamSynchronize(o->stream);
+  Graph G;
+  unsigned W;
+  if ((st = make_graph(h, num_edges, edges, weights, G, W))) return st;
+  double2* table = nullptr;
+  if ((st = upload_table(h, gamma, W, 1.0, &table))) return st;
+  unsigned grid = grid_for(h->N, 1);
+  if (h->prec == IQSG_COMPLEX_DP)
+    k_qaoa_cost_to<double><<<grid, kThreads, 0, h->stream>>>(reinterpret_cast<const double2*>(h->amps),
+                                                             reinterpret_cast<double2*>(after_cost->amps), h->N, G, table);
+  else
+    k_qaoa_cost_to<float><<<grid, kThreads, 0, h->stream>>>(reinterpret_cast<const float2*>(h->amps),
+                                                            reinterpret_cast<float2*>(after_cost->amps), h->N, G, table);
+  const double c = std::cos(beta), s = std::sin(beta);
+  for (unsigned first = 0; first < h->n; first += kQaoaWidth) {
+    LayerParams L{};
+    layer_positions(h->n, first, std::min(kQaoaWidth, h->n - first), L);
+    L.c = c;
+    L.s = s;
+    const void* src = first == 0 ? after_cost->amps : h->amps;  // first pass reads the checkpoint
+    if (h->prec == IQSG_COMPLEX_DP) dispatch_fwd<double>(h, src, L, G, table);
+    else dispatch_fwd<float>(h, src, L, G, table);
+  }
+  const size_t bytes = h->N * (h->prec == IQSG_COMPLEX_DP ? 16 : 8);
+  st = cuda_status(cudaMemcpyAsync(after_mixer->amps, h->amps, bytes, cudaMemcpyDeviceToDevice, h->stream),
+                   "iqsg_qaoa_layer_ckpt");
+  if (st) return st;
+  if (after_mixer->stream != h->stream || after_cost->stream != h->stream) cudaStreamSynchronize(h->stream);
+  return cuda_status(cudaGetLastError(), "iqsg_qaoa_layer_ckpt");
+}
+
+extern "C" int iqsg_qaoa_layer_backward_ckpt(iqsg_state* lam, const iqsg_state* after_cost,
+                                             const iqsg_state* after_mixer, unsigned num_edges, const unsigned* edges,
+                                             const int* weights, double gamma, double beta, double* grad_gamma,
+                                             double* grad_beta) {
+  int st = check_same(lam, after_cost, "iqsg_qaoa_layer_backward_ckpt");
+  if (!st) st = check_same(lam, after_mixer, "iqsg_qaoa_layer_backward_ckpt");
+  if (st) return st;
+  if (!grad_gamma || !grad_beta) return fail(IQSG_EINVAL, "iqsg_qaoa_layer_backward_ckpt: null output");
+  for (const iqsg_state* o : {after_cost, after_mixer})
+    if (o->stream != lam->stream) cudaStreamSynchronize(o->stream);
+  Graph G;
+  unsigned W;
+  if ((st = make_graph(lam, num_edges, edges, weights, G, W))) return st;
+  double2* table = nullptr;
+  if ((st = upload_table(lam, gamma, W, -1.0, &table))) return st;
+  const double c = std::cos(beta), s = -std::sin(beta);
+  double gb = 0.0, gg = 0.0;
+  for (int phase = 0; phase < 2; ++phase) {  // 0: X_q terms, 1: undo the rotations (+ H_C term)
+    for (unsigned first = 0; first < lam->n; first += kQaoaWidth) {
+      LayerParams L{};
+      layer_positions(lam->n, first, std::min(kQaoaWidth, lam->n - first), L);
+      L.c = c;
+      L.s = s;
+      L.xterms = phase == 0;
+      L.rotate = phase == 1;
+      L.cost_post = phase == 1 && first + kQaoaWidth >= lam->n;
+      L.W = W;
+      L.half_w = 0.5 * W;
+      unsigned grid = grid_for(lam->N >> L.K, 1);
+      if (grid > (unsigned)kMaxPartials) grid = kMaxPartials;
+      if (lam->prec == IQSG_COMPLEX_DP)
+        dispatch_bwd_ckpt<double>(lam, after_mixer->amps, after_cost->amps, L, G, table, grid);
+      else
+        dispatch_bwd_ckpt<float>(lam, after_mixer->amps, after_cost->amps, L, G, table, grid);
+      if (!L.xterms && !L.cost_post) continue;  // nothing summed in this pass
+      k_finish2<<<1, kThreads, 0, lam->stream>>>(lam->scratch, (int)grid, lam->scratch + kResultSlot);
+      double out[2];
+      if ((st = read2(lam, out, "iqsg_qaoa_layer_backward_ckpt"))) return st;
+      gb += out[0];
+      gg += out[1];
+    }
   }
   *grad_beta = 2.0 * gb;
   *grad_gamma = 2.0 * gg;

@@ -79,6 +79,8 @@ SIGNATURES = {
     "iqsg_qaoa_layer": [_P, _U, _UP, _IP, _D, _D],
     "iqsg_qaoa_observable": [_P, _P, _U, _UP, _IP, _DP, _DP],
     "iqsg_qaoa_layer_backward": [_P, _P, _U, _UP, _IP, _D, _D, _DP, _DP],
+    "iqsg_qaoa_layer_ckpt": [_P, _P, _P, _U, _UP, _IP, _D, _D],
+    "iqsg_qaoa_layer_backward_ckpt": [_P, _P, _P, _U, _UP, _IP, _D, _D, _DP, _DP],
     "iqsg_probability_static": [_P, _U, C.c_int, _U, _P, _P],
 }
 _RESTYPES = {"iqsg_last_error": C.c_char_p}

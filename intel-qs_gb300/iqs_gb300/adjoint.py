@@ -25,7 +25,10 @@ from .qureg import QubitRegister
 
 class QaoaMaxCut:
     def __init__(self, num_qubits: int, edges: Sequence[Tuple[int, int]], weights: Optional[Sequence[int]] = None,
-                 *, precision: str = "DP", stream: Optional[int] = None):
+                 *, precision: str = "DP", stream: Optional[int] = None, checkpoint: bool = False):
+        """checkpoint=True keeps the state after the cost phase and after the mixer of every
+        layer (2p extra vectors) so the backward pass walks only lambda back: fewer
+        operations per gradient, more memory."""
         self.n = int(num_qubits)
         self.edges = [(int(u), int(v)) for u, v in edges]
         self.weights = None if weights is None else [int(w) for w in weights]
@@ -36,6 +39,8 @@ class QaoaMaxCut:
         self.precision = precision
         self.stream = stream
         self._prepared = None  # parameters psi currently holds the circuit state of
+        self.checkpoint = checkpoint
+        self._ckpt = []
 
     def _ew(self):
         pos = np.asarray([self.psi.qubit_permutation.map[q] for q in self._edge_arr], dtype=np.uint32)
@@ -64,9 +69,30 @@ class QaoaMaxCut:
         self.prepare(gammas, betas)
         return self._observable(False)
 
+    def _grad_checkpointed(self, gammas, betas):
+        p = len(gammas)
+        while len(self._ckpt) < 2 * p:
+            self._ckpt.append(QubitRegister(self.n, "", 0, precision=self.precision, stream=self.stream))
+        self.psi.Initialize("++++", 0)
+        ne, ep, w, _keep = self._ew()
+        for l in range(p):
+            check(lib.iqsg_qaoa_layer_ckpt(self.psi._h, self._ckpt[2 * l]._h, self._ckpt[2 * l + 1]._h, ne, ep, w,
+                                           float(gammas[l]), float(betas[l])))
+        self._prepared = np.concatenate([np.asarray(gammas, float), np.asarray(betas, float)])
+        e = self._observable(True)
+        dg, db = np.zeros(p), np.zeros(p)
+        gg, gb = C.c_double(), C.c_double()
+        for l in range(p - 1, -1, -1):
+            check(lib.iqsg_qaoa_layer_backward_ckpt(self.lam._h, self._ckpt[2 * l]._h, self._ckpt[2 * l + 1]._h, ne, ep,
+                                                    w, float(gammas[l]), float(betas[l]), C.byref(gg), C.byref(gb)))
+            dg[l], db[l] = gg.value, gb.value
+        return e, dg, db
+
     def energy_and_grad(self, gammas: Sequence[float], betas: Sequence[float]):
         """Energy and its gradient by the adjoint method: (E, dE/dgamma[p], dE/dbeta[p]).
         The forward circuit is skipped when psi already holds the state of these parameters."""
+        if self.checkpoint:
+            return self._grad_checkpointed(gammas, betas)
         want = np.concatenate([np.asarray(gammas, float), np.asarray(betas, float)])
         if self._prepared is None or not np.array_equal(self._prepared, want):
             self.prepare(gammas, betas)

@@ -55,12 +55,13 @@ def iqs():
     return iqs_gb300
 
 
-def test_adjoint_matches_parameter_shift(iqs):
+@pytest.mark.parametrize("checkpoint", [False, True])
+def test_adjoint_matches_parameter_shift(iqs, checkpoint):
     n, p = 8, 3
     edges = _graph(n, 3)
     rng = np.random.default_rng(4)
     gammas, betas = rng.uniform(0, math.pi, p), rng.uniform(0, math.pi, p)
-    circ = iqs.QaoaMaxCut(n, edges)
+    circ = iqs.QaoaMaxCut(n, edges, checkpoint=checkpoint)
     e, dg, db = circ.energy_and_grad(gammas, betas)
     e_ref = _oracle_energy(n, edges, [[g] * len(edges) for g in gammas], [[b] * n for b in betas])
     assert abs(e - e_ref) <= 1e-12
@@ -118,6 +119,17 @@ def test_qaoa_layer_matches_reference_route(iqs):
             psi.ApplyRotationX(q, 2 * b)
     cut = iqs.GetExpectationValueFromCostFunction(psi, diag)
     assert abs(e - (len(edges) - 2 * cut)) <= 1e-12
+
+
+@pytest.mark.parametrize("n", [12, 17])
+def test_checkpointed_equals_plain_adjoint(iqs, n):
+    edges = [(q, (q + 1) % n) for q in range(n)] + [(q, (q + 4) % n) for q in range(0, n, 2)]
+    rng = np.random.default_rng(100 + n)
+    gammas, betas = rng.uniform(0, math.pi, 3), rng.uniform(0, math.pi, 3)
+    e0, dg0, db0 = iqs.QaoaMaxCut(n, edges).energy_and_grad(gammas, betas)
+    e1, dg1, db1 = iqs.QaoaMaxCut(n, edges, checkpoint=True).energy_and_grad(gammas, betas)
+    assert abs(e0 - e1) <= 1e-12
+    assert np.max(np.abs(np.concatenate([dg0 - dg1, db0 - db1]))) <= 1e-11
 
 
 def test_torch_autograd(iqs):
