@@ -239,6 +239,82 @@ def qaoa_section(n: int = 26, p: int = 8, stream=None) -> dict:
             "max_rel_diff_adjoint_vs_fd": rel}
 
 
+def batched_instances(count: int = 4096, seed_shape: int = 5, seed_obs: int = 6) -> list:
+    rng = np.random.default_rng(seed_shape)
+    ns = rng.integers(12, 21, size=count)
+    ls = rng.integers(4, 13, size=count)
+    orng = np.random.default_rng(seed_obs)
+    out = []
+    for n, L in zip(ns, ls):
+        terms = [(float(orng.standard_normal()), "".join(orng.choice(list("IXYZ"), size=int(n)))) for _ in range(8)]
+        out.append((int(n), int(L), terms))
+    return out
+
+
+def batched_section(count: int = 4096, loop_sample: int = 64) -> dict:
+    """Hardware-efficient ansatz batch (ComplexSP): energies + adjoint gradients of every
+    instance in one persistent launch replayed as a CUDA graph, against a per-circuit loop
+    through the public API (forward energies only, sampled and scaled), and the same batch in
+    ComplexDP as the FP64 reference for the error."""
+    import iqs_gb300 as iqs
+    inst = batched_instances(count)
+    b = iqs.BatchedAnsatz(inst, precision="SP")
+    params = np.random.default_rng(7).uniform(0, 2 * np.pi, b.num_params)
+    table = b.autotune(params, with_grad=True, trials=1)
+    best_fg = best_f = float("inf")
+    for _ in range(3):
+        t0 = time.perf_counter()
+        e32, g32 = b.run(params, with_grad=True)
+        best_fg = min(best_fg, time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        b.run(params)
+        best_f = min(best_f, time.perf_counter() - t0)
+    # FP64 reference on a subset (ComplexDP, same kernel).
+    sub = list(range(0, count, max(1, count // 256)))
+    bd = iqs.BatchedAnsatz([inst[i] for i in sub], precision="DP")
+    pd = np.concatenate([params[b.param_slices()[i]] for i in sub])
+    e64, g64 = bd.run(pd, with_grad=True)
+    g32s = np.concatenate([g32[b.param_slices()[i]] for i in sub])
+    e_err = float(np.max(np.abs(e32[sub] - e64)))
+    g_err = float(np.max(np.abs(g32s - g64)) / max(1.0, np.max(np.abs(g64))))
+    del bd
+    # Per-circuit loop through the public API, forward energy only.
+    rng = np.random.default_rng(8)
+    pick = rng.choice(count, size=min(loop_sample, count), replace=False)
+    t0 = time.perf_counter()
+    loop_e = []
+    for i in pick:
+        n, L, terms = inst[i]
+        prm = params[b.param_slices()[i]]
+        r = iqs.QubitRegister(n, "base", 0, precision="SP")
+        r.TurnOnFusion()
+        for l in range(L):
+            for q in range(n):
+                r.ApplyRotationZ(q, prm[2 * (l * n + q)])
+                r.ApplyRotationY(q, prm[2 * (l * n + q) + 1])
+            for q in range(n - 1):
+                r.ApplyCPauliZ(q, q + 1)
+        e = 0.0
+        for c, st in terms:
+            qs = [q for q, ch in enumerate(st) if ch != "I"]
+            e += r.ExpectationValue(qs, [{"X": 1, "Y": 2, "Z": 3}[st[q]] for q in qs], c) if qs else c
+        loop_e.append(e)
+    t_loop = (time.perf_counter() - t0) * count / len(pick)
+    loop_err = float(np.max(np.abs(np.asarray(loop_e) - e32[pick])))
+    gates = sum(L * (2 * n + n - 1) for n, L, _ in inst)
+    return {"workload": f"{count} hardware-efficient ansatz instances, n ~ U{{12..20}}, L ~ U{{4..12}}, "
+                        f"RZ RY per qubit + CZ ladder per layer, 8 Pauli strings each, ComplexSP",
+            "gates": gates, "parameters": int(b.num_params), "amplitudes": int(b.total_amplitudes),
+            "launch": {"threads": b.launch[0], "ctas_per_sm": b.launch[1],
+                       "autotune_s": [[t, c, round(x, 4)] for t, c, x in table]},
+            "forward_and_grad_s": round(best_fg, 4), "forward_s": round(best_f, 4),
+            "circuits_per_s_with_grad": round(count / best_fg, 1),
+            "per_circuit_loop_forward_s": round(t_loop, 3), "per_circuit_loop_sample": len(pick),
+            "speedup_forward_vs_loop": round(t_loop / best_f, 2),
+            "max_abs_energy_err_sp_vs_dp": e_err, "max_rel_grad_err_sp_vs_dp": g_err,
+            "max_abs_energy_diff_vs_loop": loop_err}
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -372,6 +448,7 @@ def run_ours(args) -> None:
     parity = None
     cpu = None
     qaoa = None
+    batched = None
     if rank == 0:
         import oracle
         oracle.build(ref=False)
@@ -391,6 +468,7 @@ def run_ours(args) -> None:
             threads = os.cpu_count() or 1
             cpu = cpu_layer_gbs(args.cpu_qubits, 1, seed=5, threads=threads)
         qaoa = None if args.no_adjoint else qaoa_section(stream=stream.cuda_stream)
+        batched = None if args.no_batched else batched_section()
 
     if rank == 0:
         dtype = "c128: f64 storage, double-float (fp32x2) products and sums" if args.math == "emulated" else "f64"
@@ -422,6 +500,8 @@ def run_ours(args) -> None:
         line.update(other)
         if qaoa is not None:
             line["adjoint"] = qaoa
+        if batched is not None:
+            line["batched"] = batched
         if cpu is not None:
             line["cpu_baseline"] = {"value": round(cpu["gbs"], 3), "unit": UNIT, "cores": cpu["cores"],
                                     "kind": cpu["kind"],
@@ -449,6 +529,7 @@ def main() -> None:
     ap.add_argument("--pipeline", type=int, default=0, help="with --width: 1 = bulk-copy pipelined passes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the QAOA adjoint-gradient section")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-circuits section")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per 1-qubit-gate launch from an ncu capture, if known")
     args = ap.parse_args()

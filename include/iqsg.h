@@ -284,6 +284,41 @@ int iqsg_qaoa_layer_backward_ckpt(iqsg_state* lam, const iqsg_state* after_cost,
                                   unsigned num_edges, const unsigned* edges, const int* weights, double gamma,
                                   double beta, double* grad_gamma, double* grad_beta);
 
+/* ---- batches of small circuits --------------------------------------------------------- */
+
+/* One Pauli string of an observable, in data positions: xmask = positions with X or Y,
+ * zmask = positions with Y or Z, ny = number of Y factors mod 4; P|y> = i^ny (-1)^|y & zmask|
+ * |y ^ xmask>. */
+typedef struct {
+  uint64_t xmask, zmask;
+  int32_t ny;
+  int32_t pad;
+  double coeff;
+} iqsg_pauli_term;
+
+typedef struct iqsg_batch iqsg_batch;
+
+/* A batch of count hardware-efficient ansatz instances: instance i has num_qubits[i] (<= 24)
+ * qubits and num_layers[i] layers, each layer RZ(phi) then RY(theta) on every qubit and CZ(q,
+ * q+1) for q = 0..n-2, starting from |0..0>; its observable is terms_per_instance[i] Pauli
+ * strings, taken in order from terms. Parameters per instance: [layer][qubit][phi, theta].
+ * Allocates two state vectors per instance. No counterpart in the reference. */
+int iqsg_batch_create(unsigned count, const unsigned* num_qubits, const unsigned* num_layers,
+                      const unsigned* terms_per_instance, const iqsg_pauli_term* terms, int precision,
+                      void* stream, iqsg_batch** out);
+int iqsg_batch_destroy(iqsg_batch* b);
+
+/* Evaluate every instance in one persistent launch (CTAs pull instances, largest first, from
+ * a work counter), recorded once into a CUDA graph and replayed on later calls: energies[i],
+ * and with with_grad the adjoint-mode gradient of every parameter (same layout as params).
+ * params, energies and grads are host arrays. */
+int iqsg_batch_run(iqsg_batch* b, const double* params, int with_grad, double* energies, double* grads);
+
+/* Launch shape of the persistent kernel (threads per CTA, CTAs per SM); chosen by the
+ * autotuner. Invalidates the recorded graphs. */
+int iqsg_batch_set_launch(iqsg_batch* b, unsigned threads, unsigned ctas_per_sm);
+int iqsg_batch_info(const iqsg_batch* b, uint64_t* num_params, uint64_t* total_amplitudes);
+
 /* ---- allocation-free measurement -------------------------------------------------------- */
 
 /* Probability of |1> on position pos (sum of |amp|^2 over indices with that bit set) for

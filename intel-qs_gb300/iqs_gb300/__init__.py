@@ -12,6 +12,7 @@ from ._lib import IqsgError, LIB_PATH, lib
 from .permutation import GateCounter, Permutation
 from .qureg import QubitRegister
 from .adjoint import QaoaMaxCut, qaoa_energy
+from .batched import BatchedAnsatz
 from .qaoa import (GetExpectationValueFromCostFunction, GetExpectationValueSquaredFromCostFunction,
                    ImplementQaoaLayerBasedOnCostFunction, InitializeVectorAsMaxCutCostFunction)
 
@@ -19,5 +20,5 @@ __all__ = [
     "QubitRegister", "Permutation", "GateCounter", "IqsgError", "LIB_PATH", "lib",
     "InitializeVectorAsMaxCutCostFunction", "ImplementQaoaLayerBasedOnCostFunction",
     "GetExpectationValueFromCostFunction", "GetExpectationValueSquaredFromCostFunction",
-    "QaoaMaxCut", "qaoa_energy",
+    "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz",
 ]

@@ -36,6 +36,15 @@ class Op(C.Structure):
 
 assert C.sizeof(Op) == 304, "iqsg_op layout mismatch"
 
+
+class PauliTerm(C.Structure):
+    """iqsg_pauli_term (include/iqsg.h)."""
+    _fields_ = [("xmask", C.c_uint64), ("zmask", C.c_uint64), ("ny", C.c_int32), ("pad", C.c_int32),
+                ("coeff", C.c_double)]
+
+
+assert C.sizeof(PauliTerm) == 32, "iqsg_pauli_term layout mismatch"
+
 # name -> argtypes (every function returns int status unless listed in _RESTYPES)
 SIGNATURES = {
     "iqsg_last_error": [],
@@ -81,6 +90,11 @@ SIGNATURES = {
     "iqsg_qaoa_layer_backward": [_P, _P, _U, _UP, _IP, _D, _D, _DP, _DP],
     "iqsg_qaoa_layer_ckpt": [_P, _P, _P, _U, _UP, _IP, _D, _D],
     "iqsg_qaoa_layer_backward_ckpt": [_P, _P, _P, _U, _UP, _IP, _D, _D, _DP, _DP],
+    "iqsg_batch_create": [_U, _UP, _UP, _UP, C.POINTER(PauliTerm), C.c_int, _P, C.POINTER(_P)],
+    "iqsg_batch_destroy": [_P],
+    "iqsg_batch_run": [_P, _DP, C.c_int, _DP, _DP],
+    "iqsg_batch_set_launch": [_P, _U, _U],
+    "iqsg_batch_info": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
     "iqsg_probability_static": [_P, _U, C.c_int, _U, _P, _P],
 }
 _RESTYPES = {"iqsg_last_error": C.c_char_p}
