@@ -174,7 +174,10 @@ typedef enum {
   IQSG_OP_2Q = 2,       /* dense 4x4 m, row/column index 2*b(t0) + b(t1) */
   IQSG_OP_SWAPLIKE = 3, /* 2x2 m on the {|lo=1,hi=0>, |lo=0,hi=1>} pair of positions t0, t1 */
   IQSG_OP_DIAG2 = 4,    /* amp *= m[2*b(t0) + b(t1)] (4 complex entries) */
-  IQSG_OP_PHASE = 5     /* amp *= m[0] where (index & mask) == value */
+  IQSG_OP_PHASE = 5,    /* amp *= m[0] where (index & mask) == value */
+  IQSG_OP_GRAD1 = 6,    /* iqsg_adjoint_ops only: grads[value] += Im <lam|M|psi>, M = 2x2 m on t0 */
+  IQSG_OP_GRAD2 = 7     /* iqsg_adjoint_ops only: grads[value] += Im <lam|M|psi>, M = 4x4 m,
+                           row/column index 2*b(t0) + b(t1) */
 } iqsg_op_kind;
 
 typedef struct {
@@ -194,6 +197,19 @@ typedef struct {
  * Replaces the reference's cache-blocked replay of buffered gates, ApplyFusedGates:
  * src/qureg_fusion.cpp:55-94. */
 int iqsg_apply_ops(iqsg_state* h, const iqsg_op* ops, unsigned count, unsigned* sweeps);
+
+/* Reverse-mode (adjoint) gradients over two registers of equal size and precision: psi (the
+ * circuit state after the gates) and lam (the adjoint state, O psi for E = <psi|O|psi>).
+ * The ops list the circuit backwards: for each gate G = exp(-i theta A), first (if theta
+ * depends on a parameter) an IQSG_OP_GRAD1/GRAD2 op with M = 2 (d theta / d param) A and
+ * value = the parameter index, then G^dagger as a gate op. Gate ops act on both registers;
+ * a gradient op adds Im <lam|M|psi> over the whole state into grads[value], which is that
+ * gate's share of dE/dparam. Everything is packed into fused two-vector sweeps; sums are
+ * FP64 in a fixed order. grads (nparams <= 2048 host doubles) is added to, not overwritten.
+ * ComplexDP runs in native FP64 arithmetic whatever iqsg_set_math chose. Waits for the
+ * result. The reference has no adjoint path: its gradients come from re-running circuits. */
+int iqsg_adjoint_ops(iqsg_state* psi, iqsg_state* lam, const iqsg_op* ops, unsigned count, double* grads,
+                     unsigned nparams, unsigned* sweeps);
 
 /* Largest number of target positions per sweep (1..4; 0 restores the default: 4 for
  * ComplexSP, 3 for native ComplexDP, 2 for emulated ComplexDP, which is capped at 3).

@@ -106,6 +106,10 @@ Positions sorted_positions(std::vector<unsigned> v) {
   return z;
 }
 
+}  // namespace
+
+namespace iqsg {
+
 // A kernel whose bounded wait ran out leaves a nonzero word at scratch[kErrorSlot]; the
 // next call that waits for the stream reports it (and clears it).
 int take_device_error(iqsg_state* h, unsigned long long word, const char* what) {
@@ -141,6 +145,10 @@ int sync_and_check(iqsg_state* h, const char* what) {
   std::memcpy(&word, h->host_result + 8, sizeof word);
   return take_device_error(h, word, what);
 }
+
+}  // namespace iqsg
+
+namespace {
 
 template <typename F>
 int dispatch(const iqsg_state* h, F&& f) {

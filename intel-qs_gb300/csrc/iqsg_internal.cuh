@@ -47,6 +47,9 @@ int cuda_status(cudaError_t e, const char* what);
 // Grid size for a grid-stride loop over `work` items, `per_thread` items per thread.
 unsigned grid_for(uint64_t work, int per_thread);
 int num_sms();
+// Wait for the register's stream and report a device error word left by a bounded wait.
+int sync_and_check(iqsg_state* h, const char* what);
+int take_device_error(iqsg_state* h, unsigned long long word, const char* what);
 
 template <typename R> struct V2;
 template <> struct V2<double> { using type = double2; };

@@ -50,6 +50,7 @@ namespace iqsg {
 namespace {
 
 constexpr unsigned kMaxBatchQubits = 24;
+constexpr unsigned kChunk = 16;  // pairs per R-precision partial of a gradient sum
 
 template <typename R>
 struct CXb {
@@ -219,7 +220,11 @@ __global__ void k_batched(unsigned count, const unsigned* __restrict__ order, co
         sincos(0.5 * theta, &st, &ct);
         sincos(0.5 * phi, &sp, &cp);
         const R c = (R)ct, s = (R)st, zc = (R)cp, zs = (R)sp;
+        // Products and short partial sums in R; every kChunk pairs the partials move into FP64
+        // (FP64 arithmetic per pair would bound the pass on the FP64 pipe).
         double gy = 0.0, gz = 0.0;
+        R cy = 0, cz = 0;
+        unsigned cnt = 0;
         for (uint64_t pidx = tid; pidx < half; pidx += nth) {
           const uint64_t i0 = insert_zero(pidx, q), i1 = i0 | d;
           V p0 = psi[i0], p1 = psi[i1], l0 = lam[i0], l1 = lam[i1];
@@ -228,7 +233,7 @@ __global__ void k_batched(unsigned count, const unsigned* __restrict__ order, co
             if (__popcll(i1 & (i1 >> 1) & ladder) & 1) { p1.x = -p1.x; p1.y = -p1.y; l1.x = -l1.x; l1.y = -l1.y; }
           }
           // RY(theta): Im <lambda|Y_q|psi> = -Re(conj(l0) p1) + Re(conj(l1) p0), then undo RY.
-          gy += -((double)l0.x * p1.x + (double)l0.y * p1.y) + ((double)l1.x * p0.x + (double)l1.y * p0.y);
+          cy += (l1.x * p0.x + l1.y * p0.y) - (l0.x * p1.x + l0.y * p1.y);
           V a0, a1, b0, b1;
           a0.x = c * p0.x + s * p1.x; a0.y = c * p0.y + s * p1.y;
           a1.x = c * p1.x - s * p0.x; a1.y = c * p1.y - s * p0.y;
@@ -236,13 +241,21 @@ __global__ void k_batched(unsigned count, const unsigned* __restrict__ order, co
           b1.x = c * l1.x - s * l0.x; b1.y = c * l1.y - s * l0.y;
           // RZ(phi): Im <lambda|Z_q|psi> (bit 0: +, bit 1: -), then undo RZ
           // (multiply by e^{+i phi/2} on bit 0, e^{-i phi/2} on bit 1).
-          gz += ((double)b0.x * a0.y - (double)b0.y * a0.x) - ((double)b1.x * a1.y - (double)b1.y * a1.x);
+          cz += (b0.x * a0.y - b0.y * a0.x) - (b1.x * a1.y - b1.y * a1.x);
+          if (++cnt == kChunk) {
+            gy += (double)cy;
+            gz += (double)cz;
+            cy = cz = 0;
+            cnt = 0;
+          }
           V o;
           o.x = zc * a0.x - zs * a0.y; o.y = zc * a0.y + zs * a0.x; psi[i0] = o;
           o.x = zc * a1.x + zs * a1.y; o.y = zc * a1.y - zs * a1.x; psi[i1] = o;
           o.x = zc * b0.x - zs * b0.y; o.y = zc * b0.y + zs * b0.x; lam[i0] = o;
           o.x = zc * b1.x + zs * b1.y; o.y = zc * b1.y - zs * b1.x; lam[i1] = o;
         }
+        gy += (double)cy;
+        gz += (double)cz;
         block_sum2(gy, gz, s_red);
         if (tid == 0) {
           grd[2 * (l * n + q) + 1] = gy;

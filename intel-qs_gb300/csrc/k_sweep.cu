@@ -109,6 +109,90 @@ __global__ void __launch_bounds__(kThreads) k_sweep_df(double2* __restrict__ s, 
   }
 }
 
+// ---- adjoint sweep: psi and lambda together, gradient sums per slot -------------------------
+//
+// Gradient terms are summed in R over kGradChunk groups, then moved into FP64 per thread;
+// per-block sums (fixed-order warp and block trees) land in partials[block * kGradSlots + s].
+// The grid is fixed by the register size, so the order of every sum is too.
+constexpr unsigned kGradChunk = 16;
+constexpr unsigned kAdjBlocksPerSm = 2;
+
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_sweep_adj(typename V2<R>::type* __restrict__ psi,
+                                                        typename V2<R>::type* __restrict__ lam, uint64_t ngroups,
+                                                        const __grid_constant__ SweepParams P, unsigned nslots,
+                                                        double* __restrict__ partials) {
+  constexpr int G = 1 << K;
+  using A = NativeArith<R>;
+  R racc[kGradSlots];
+  double dacc[kGradSlots];
+#pragma unroll
+  for (int k = 0; k < kGradSlots; ++k) {
+    racc[k] = 0;
+    dacc[k] = 0.0;
+  }
+  unsigned cnt = 0;
+  for (uint64_t g = gtid(); g < ngroups; g += gstride()) {
+    uint64_t idx[G];
+    group_indices<K>(P, g, idx);
+    typename A::VT v[G], w[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const auto a = psi[idx[k]], b = lam[idx[k]];
+      v[k].re = a.x;
+      v[k].im = a.y;
+      w[k].re = b.x;
+      w[k].im = b.y;
+    }
+    unsigned tm = 0;
+    run_ops_dual<R, K>(P, v, w, idx, tm, racc);
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      if (!(tm & (1u << k))) continue;
+      typename V2<R>::type a, b;
+      a.x = v[k].re;
+      a.y = v[k].im;
+      b.x = w[k].re;
+      b.y = w[k].im;
+      psi[idx[k]] = a;
+      lam[idx[k]] = b;
+    }
+    if (++cnt == kGradChunk) {
+      cnt = 0;
+      for (unsigned k = 0; k < nslots; ++k) {
+        dacc[k] += (double)racc[k];
+        racc[k] = 0;
+      }
+    }
+  }
+  __shared__ double red[kThreads / 32][kGradSlots];
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (unsigned k = 0; k < nslots; ++k) {
+    double x = dacc[k] + (double)racc[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < nslots) {
+    double t = 0.0;
+    for (unsigned w = 0; w < kThreads / 32; ++w) t += red[w][threadIdx.x];
+    partials[(uint64_t)blockIdx.x * kGradSlots + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_grad_finish(const double* __restrict__ partials, unsigned nblocks, const GradMap map,
+                              double* __restrict__ grad) {
+  __shared__ double tot[kGradSlots];
+  if (threadIdx.x < map.nslots) {
+    double t = 0.0;
+    for (unsigned b = 0; b < nblocks; ++b) t += partials[(uint64_t)b * kGradSlots + threadIdx.x];
+    tot[threadIdx.x] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (unsigned k = 0; k < map.nslots; ++k) grad[map.param[k]] += tot[k];  // two slots may share a parameter
+}
+
 // ---- bulk-copy pipelined sweep (large registers) ------------------------------------------
 //
 // A persistent grid streams tiles through shared memory: thread 0 keeps kTmaStages - 1 tiles
@@ -360,6 +444,38 @@ void launch_sweep(iqsg_state* h, const SweepParams& P) {
   }
 }
 
+namespace {
+
+template <int K>
+void launch_adj_k(iqsg_state* psi, iqsg_state* lam, const SweepParams& P, const GradMap& map, double* grad) {
+  const uint64_t ngroups = psi->N >> K;
+  uint64_t blocks = (ngroups + kThreads - 1) / kThreads;
+  const uint64_t cap = (uint64_t)num_sms() * kAdjBlocksPerSm;
+  if (blocks > cap) blocks = cap;
+  if (blocks * kGradSlots > 2 * (uint64_t)kMaxPartials) blocks = 2 * kMaxPartials / kGradSlots;
+  double* partials = psi->scratch;
+  if (psi->prec == IQSG_COMPLEX_SP)
+    k_sweep_adj<float, K><<<(unsigned)blocks, kThreads, 0, psi->stream>>>(
+        reinterpret_cast<float2*>(psi->amps), reinterpret_cast<float2*>(lam->amps), ngroups, P, map.nslots, partials);
+  else
+    k_sweep_adj<double, K><<<(unsigned)blocks, kThreads, 0, psi->stream>>>(
+        reinterpret_cast<double2*>(psi->amps), reinterpret_cast<double2*>(lam->amps), ngroups, P, map.nslots,
+        partials);
+  if (map.nslots) k_grad_finish<<<1, 32, 0, psi->stream>>>(partials, (unsigned)blocks, map, grad);
+}
+
+}  // namespace
+
+void launch_sweep_adj(iqsg_state* psi, iqsg_state* lam, const SweepParams& P, const GradMap& map, double* grad) {
+  switch (P.K) {
+    case 0: launch_adj_k<0>(psi, lam, P, map, grad); break;
+    case 1: launch_adj_k<1>(psi, lam, P, map, grad); break;
+    case 2: launch_adj_k<2>(psi, lam, P, map, grad); break;
+    case 3: launch_adj_k<3>(psi, lam, P, map, grad); break;
+    case 4: launch_adj_k<4>(psi, lam, P, map, grad); break;
+  }
+}
+
 // ---------------------------------------------------------------------------------------
 // Scheduler: greedy packing of a gate stream into sweeps.
 // ---------------------------------------------------------------------------------------
@@ -394,6 +510,11 @@ bool is_x(const double* m) {
 class SweepBuilder {
  public:
   SweepBuilder(iqsg_state* h, unsigned kmax) : h_(h), kmax_(kmax) { reset(); }
+  // Adjoint mode: every gate acts on h and lam; gradient operations add into grad[param].
+  SweepBuilder(iqsg_state* h, iqsg_state* lam, double* grad, unsigned kmax)
+      : h_(h), lam_(lam), grad_(grad), kmax_(kmax) {
+    reset();
+  }
 
   // Slot of position p in the current sweep, or -1 when p is not active.
   int slot(unsigned p) {
@@ -402,7 +523,7 @@ class SweepBuilder {
     return -1;
   }
 
-  bool fits(const std::vector<unsigned>& targets, unsigned ops, unsigned entries) const {
+  bool fits(const std::vector<unsigned>& targets, unsigned ops, unsigned entries, unsigned slots = 0) const {
     unsigned add = 0;
     for (unsigned t : targets) {
       bool have = false;
@@ -412,12 +533,12 @@ class SweepBuilder {
     // A two-position operation opens a 2-wide sweep even when the width limit is 1.
     const unsigned kmax = std::max<unsigned>(kmax_, (unsigned)targets.size());
     return P_.K + add <= kmax && P_.nops + ops <= (unsigned)kSweepMaxOps &&
-           nent_ + entries <= (unsigned)kSweepMaxEntries;
+           nent_ + entries <= (unsigned)kSweepMaxEntries && map_.nslots + slots <= (unsigned)kGradSlots;
   }
 
   // Make room (flushing if necessary) and activate the target positions.
-  void reserve(const std::vector<unsigned>& targets, unsigned ops, unsigned entries) {
-    if (!fits(targets, ops, entries)) flush();
+  void reserve(const std::vector<unsigned>& targets, unsigned ops, unsigned entries, unsigned slots = 0) {
+    if (!fits(targets, ops, entries, slots)) flush();
     for (unsigned t : targets)
       if (slot(t) < 0) P_.pos[P_.K++] = t;
   }
@@ -460,14 +581,36 @@ class SweepBuilder {
   }
 
   void add_u4(unsigned ph, unsigned pl, const double* m) {
-    bool diag = true;
+    auto z = [&](int r, int c) { return is_zero(m[2 * (4 * r + c)], m[2 * (4 * r + c) + 1]); };
+    bool diag = true, excitation = true;  // excitation: |00> and |11> only pick up phases
     for (int r = 0; r < 4; ++r)
-      for (int c = 0; c < 4; ++c)
-        if (r != c && !is_zero(m[2 * (4 * r + c)], m[2 * (4 * r + c) + 1])) diag = false;
+      for (int c = 0; c < 4; ++c) {
+        if (r != c && !z(r, c)) diag = false;
+        const bool inner = (r == 1 || r == 2) && (c == 1 || c == 2);
+        if (r != c && !inner && !z(r, c)) excitation = false;
+      }
     const uint64_t bh = uint64_t(1) << ph, bl = uint64_t(1) << pl;
     if (diag) {
       for (int k = 0; k < 4; ++k)
         add_phase(bh | bl, ((k & 2) ? bh : 0) | ((k & 1) ? bl : 0), m[2 * (5 * k)], m[2 * (5 * k) + 1]);
+      return;
+    }
+    if (excitation) {
+      // Phases on |00> and |11>, a 2x2 on {|01>, |10>} (rows/columns 1 = low bit set, 2 = high bit set).
+      add_phase(bh | bl, 0, m[0], m[1]);
+      add_phase(bh | bl, bh | bl, m[30], m[31]);
+      auto e = [&](int r, int c, double* o) {
+        o[0] = m[2 * (4 * r + c)];
+        o[1] = m[2 * (4 * r + c) + 1];
+      };
+      double w[8];
+      // add_swaplike orders the pair as (lower position set, higher position set).
+      const int a = pl < ph ? 1 : 2, b = pl < ph ? 2 : 1;
+      e(a, a, w);
+      e(a, b, w + 2);
+      e(b, a, w + 4);
+      e(b, b, w + 6);
+      add_swaplike(pl, ph, w);
       return;
     }
     reserve({ph, pl}, 1, 16);
@@ -491,11 +634,28 @@ class SweepBuilder {
     P_.ops[P_.nops++] = op;
   }
 
+  // Adjoint mode: add Im <lam|M|psi> on the target positions into grad[param]; M is 2x2
+  // (one target) or 4x4 (rows 2*b(t0) + b(t1)).
+  void add_grad(unsigned ntargets, unsigned t0, unsigned t1, const double* m, unsigned param) {
+    const unsigned ne = ntargets == 1 ? 4u : 16u;
+    if (ntargets == 1) reserve({t0}, 1, ne, 1);
+    else reserve({t0, t1}, 1, ne, 1);
+    SweepOp op{};
+    op.kind = ntargets == 1 ? SW_GRAD1 : SW_GRAD2;
+    op.j0 = (uint8_t)slot(t0);
+    op.j1 = ntargets == 1 ? 0 : (uint8_t)slot(t1);
+    op.value = map_.nslots;
+    map_.param[map_.nslots++] = param;
+    op.ent = add_entries(m, ne);
+    P_.ops[P_.nops++] = op;
+  }
+
   void flush() {
     if (P_.nops) {
       std::copy(P_.pos, P_.pos + P_.K, P_.sorted);
       std::sort(P_.sorted, P_.sorted + P_.K);
-      launch_sweep(h_, P_);
+      if (lam_) launch_sweep_adj(h_, lam_, P_, map_, grad_);
+      else launch_sweep(h_, P_);
       ++launched_;
     }
     reset();
@@ -506,9 +666,13 @@ class SweepBuilder {
  private:
   void reset() {
     std::memset(&P_, 0, sizeof(P_));
+    std::memset(&map_, 0, sizeof(map_));
     nent_ = 0;
   }
   iqsg_state* h_;
+  iqsg_state* lam_ = nullptr;
+  double* grad_ = nullptr;
+  GradMap map_;
   unsigned kmax_;
   SweepParams P_;
   unsigned nent_ = 0;
@@ -534,7 +698,8 @@ using namespace iqsg;
 
 namespace {
 
-int check_op(const iqsg_state* h, const iqsg_op& op, unsigned i) {
+// adjoint: the op list of iqsg_adjoint_ops (gradient ops allowed, parameter index < nparams).
+int check_op(const iqsg_state* h, const iqsg_op& op, unsigned i, bool adjoint = false, unsigned nparams = 0) {
   auto bad = [&](const char* why) { return fail(IQSG_EINVAL, "iqsg_apply_ops: op %u: %s", i, why); };
   uint64_t seen = 0;
   auto use = [&](unsigned p) {
@@ -562,10 +727,53 @@ int check_op(const iqsg_state* h, const iqsg_op& op, unsigned i) {
       if (h->n < 64 && ((op.mask >> h->n) != 0)) return bad("phase mask beyond the register");
       if ((op.value & ~op.mask) != 0) return bad("phase value outside its mask");
       break;
+    case IQSG_OP_GRAD1:
+    case IQSG_OP_GRAD2:
+      if (!adjoint) return bad("gradient ops belong to iqsg_adjoint_ops");
+      if (op.value >= nparams) return bad("parameter index out of range");
+      if (!use(op.t0)) return bad("target out of range");
+      if (op.kind == IQSG_OP_GRAD2 && !use(op.t1)) return bad("positions out of range or equal");
+      break;
     default:
       return bad("unknown kind");
   }
   return IQSG_OK;
+}
+
+// Queue one validated gate op on a builder.
+void queue_op(SweepBuilder& b, const iqsg_op& op) {
+  switch (op.kind) {
+    case IQSG_OP_1Q:
+      b.add_u2(op.t0, 0, op.m);
+      break;
+    case IQSG_OP_CTRL: {
+      uint64_t cm = 0;
+      for (unsigned c = 0; c < op.nctrl; ++c) cm |= uint64_t(1) << op.ctrl[c];
+      b.add_u2(op.t0, cm, op.m);
+      break;
+    }
+    case IQSG_OP_2Q:
+      b.add_u4(op.t0, op.t1, op.m);
+      break;
+    case IQSG_OP_SWAPLIKE:
+      b.add_swaplike(op.t0, op.t1, op.m);
+      break;
+    case IQSG_OP_DIAG2: {
+      const uint64_t b1 = uint64_t(1) << op.t0, b2 = uint64_t(1) << op.t1;
+      for (int k = 0; k < 4; ++k)
+        b.add_phase(b1 | b2, ((k & 2) ? b1 : 0) | ((k & 1) ? b2 : 0), op.m[2 * k], op.m[2 * k + 1]);
+      break;
+    }
+    case IQSG_OP_PHASE:
+      b.add_phase(op.mask, op.value, op.m[0], op.m[1]);
+      break;
+    case IQSG_OP_GRAD1:
+      b.add_grad(1, op.t0, 0, op.m, (unsigned)op.value);
+      break;
+    case IQSG_OP_GRAD2:
+      b.add_grad(2, op.t0, op.t1, op.m, (unsigned)op.value);
+      break;
+  }
 }
 
 }  // namespace
@@ -598,36 +806,42 @@ extern "C" int iqsg_apply_ops(iqsg_state* h, const iqsg_op* ops, unsigned count,
     if (st) return st;
   }
   SweepBuilder b(h, std::max(1u, sweep_width(h)));
-  for (unsigned i = 0; i < count; ++i) {
-    const iqsg_op& op = ops[i];
-    switch (op.kind) {
-      case IQSG_OP_1Q:
-        b.add_u2(op.t0, 0, op.m);
-        break;
-      case IQSG_OP_CTRL: {
-        uint64_t cm = 0;
-        for (unsigned c = 0; c < op.nctrl; ++c) cm |= uint64_t(1) << op.ctrl[c];
-        b.add_u2(op.t0, cm, op.m);
-        break;
-      }
-      case IQSG_OP_2Q:
-        b.add_u4(op.t0, op.t1, op.m);
-        break;
-      case IQSG_OP_SWAPLIKE:
-        b.add_swaplike(op.t0, op.t1, op.m);
-        break;
-      case IQSG_OP_DIAG2: {
-        const uint64_t b1 = uint64_t(1) << op.t0, b2 = uint64_t(1) << op.t1;
-        for (int k = 0; k < 4; ++k)
-          b.add_phase(b1 | b2, ((k & 2) ? b1 : 0) | ((k & 1) ? b2 : 0), op.m[2 * k], op.m[2 * k + 1]);
-        break;
-      }
-      case IQSG_OP_PHASE:
-        b.add_phase(op.mask, op.value, op.m[0], op.m[1]);
-        break;
-    }
-  }
+  for (unsigned i = 0; i < count; ++i) queue_op(b, ops[i]);
   b.flush();
   if (sweeps) *sweeps = b.launched();
   return cuda_status(cudaGetLastError(), "iqsg_apply_ops");
+}
+
+extern "C" int iqsg_adjoint_ops(iqsg_state* psi, iqsg_state* lam, const iqsg_op* ops, unsigned count, double* grads,
+                                unsigned nparams, unsigned* sweeps) {
+  if (!psi || !lam) return fail(IQSG_EINVAL, "null register handle");
+  if (psi == lam) return fail(IQSG_EINVAL, "iqsg_adjoint_ops: psi and lam must be different registers");
+  if (psi->n != lam->n || psi->prec != lam->prec || psi->device != lam->device)
+    return fail(IQSG_EINVAL, "iqsg_adjoint_ops: registers differ in size, precision or device");
+  if (count && !ops) return fail(IQSG_EINVAL, "iqsg_adjoint_ops: null op array");
+  if (nparams > (unsigned)kTableDoubles) return fail(IQSG_EINVAL, "iqsg_adjoint_ops: more than %d parameters", kTableDoubles);
+  if (nparams && !grads) return fail(IQSG_EINVAL, "iqsg_adjoint_ops: null gradient array");
+  for (unsigned i = 0; i < count; ++i) {
+    const int st = check_op(psi, ops[i], i, true, nparams);
+    if (st) return st;
+  }
+  int st = IQSG_OK;
+  if (lam->stream != psi->stream && (st = sync_and_check(lam, "iqsg_adjoint_ops"))) return st;
+  double* dgrad = psi->scratch + kTableSlot;
+  if (nparams && (st = cuda_status(cudaMemsetAsync(dgrad, 0, sizeof(double) * nparams, psi->stream),
+                                   "iqsg_adjoint_ops: clear")))
+    return st;
+  const unsigned kmax = std::max(1u, std::min(sweep_width(psi), psi->prec == IQSG_COMPLEX_SP ? 4u : 3u));
+  SweepBuilder b(psi, lam, dgrad, kmax);
+  for (unsigned i = 0; i < count; ++i) queue_op(b, ops[i]);
+  b.flush();
+  if (sweeps) *sweeps = b.launched();
+  if ((st = cuda_status(cudaGetLastError(), "iqsg_adjoint_ops"))) return st;
+  std::vector<double> g(nparams);
+  if (nparams && (st = cuda_status(cudaMemcpyAsync(g.data(), dgrad, sizeof(double) * nparams, cudaMemcpyDeviceToHost,
+                                                   psi->stream), "iqsg_adjoint_ops: gradients")))
+    return st;
+  if ((st = sync_and_check(psi, "iqsg_adjoint_ops"))) return st;
+  for (unsigned k = 0; k < nparams; ++k) grads[k] += g[k];
+  return IQSG_OK;
 }

@@ -19,12 +19,15 @@ namespace iqsg {
 constexpr int kSweepMaxK = 4;
 constexpr int kSweepMaxOps = 48;
 constexpr int kSweepMaxEntries = 160;
+constexpr int kGradSlots = 16;  // gradient accumulators per adjoint sweep
 
 enum SweepKind : uint8_t {
   SW_U2 = 0,        // 2x2 on active bit j0, applied where (idx & mask) == mask
   SW_PHASE = 1,     // amp *= entry where (idx & mask) == value
   SW_U4 = 2,        // 4x4 on active bits (j0 = high, j1 = low), where (idx & mask) == mask
   SW_SWAPLIKE = 3,  // 2x2 on the (j0 = 1, j1 = 0) / (j0 = 0, j1 = 1) pair, where (idx & mask) == mask
+  SW_GRAD1 = 4,     // adjoint sweeps only: accumulate Im <w|M|v>, M 2x2 on j0
+  SW_GRAD2 = 5,     // adjoint sweeps only: accumulate Im <w|M|v>, M 4x4 on (j0 high, j1 low)
 };
 
 enum SweepFlags : uint8_t {
@@ -191,10 +194,10 @@ __device__ __forceinline__ void vt_mul_i(VT& a, bool plus) {
 // ---- the op interpreter -----------------------------------------------------------------
 
 template <typename A, int K, int J>
-__device__ __forceinline__ void op_u2(const SweepParams& P, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
+__device__ __forceinline__ void op_u2(const SweepEntry* E, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
                                       unsigned& tm) {
   constexpr int G = 1 << K, B = 1 << J;
-  const SweepEntry* m = P.ent + op.ent;
+  const SweepEntry* m = E + op.ent;
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & B) continue;
@@ -212,10 +215,10 @@ __device__ __forceinline__ void op_u2(const SweepParams& P, const SweepOp& op, t
 }
 
 template <typename A, int K, int JH, int JL>
-__device__ __forceinline__ void op_u4(const SweepParams& P, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
+__device__ __forceinline__ void op_u4(const SweepEntry* E, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
                                       unsigned& tm) {
   constexpr int G = 1 << K, BH = 1 << JH, BL = 1 << JL;
-  const SweepEntry* m = P.ent + op.ent;
+  const SweepEntry* m = E + op.ent;
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & (BH | BL)) continue;
@@ -230,10 +233,10 @@ __device__ __forceinline__ void op_u4(const SweepParams& P, const SweepOp& op, t
 }
 
 template <typename A, int K, int JLO, int JHI>
-__device__ __forceinline__ void op_swaplike(const SweepParams& P, const SweepOp& op, typename A::VT* v,
+__device__ __forceinline__ void op_swaplike(const SweepEntry* E, const SweepOp& op, typename A::VT* v,
                                             const uint64_t* idx, unsigned& tm) {
   constexpr int G = 1 << K, BL = 1 << JLO, BH = 1 << JHI;
-  const SweepEntry* m = P.ent + op.ent;
+  const SweepEntry* m = E + op.ent;
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & (BH | BL)) continue;
@@ -251,10 +254,10 @@ __device__ __forceinline__ void op_swaplike(const SweepParams& P, const SweepOp&
 }
 
 template <typename A, int K>
-__device__ __forceinline__ void op_phase(const SweepParams& P, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
+__device__ __forceinline__ void op_phase(const SweepEntry* E, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
                                          unsigned& tm) {
   constexpr int G = 1 << K;
-  const SweepEntry& f = P.ent[op.ent];
+  const SweepEntry& f = E[op.ent];
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if ((idx[s] & op.mask) != op.value) continue;
@@ -266,50 +269,156 @@ __device__ __forceinline__ void op_phase(const SweepParams& P, const SweepOp& op
   }
 }
 
-// Apply every operation of the sweep to one group, in order. Bit s of tm records that slot s
-// was written. A runtime active-bit index is dispatched to a compile-time one, so the group
-// stays in registers (no dynamic register indexing).
+// One operation on one group. A runtime active-bit index is dispatched to a compile-time
+// one, so the group stays in registers (no dynamic register indexing).
 template <typename A, int K>
-__device__ __forceinline__ void run_ops(const SweepParams& P, typename A::VT* v, const uint64_t* idx, unsigned& tm) {
-#pragma unroll 1
-  for (unsigned o = 0; o < P.nops; ++o) {
-    const SweepOp op = P.ops[o];
-    switch (op.kind) {
-      case SW_PHASE:
-        op_phase<A, K>(P, op, v, idx, tm);
-        break;
-      case SW_U2:
-        if constexpr (K >= 1) {
-          switch (op.j0) {
-            case 0: op_u2<A, K, 0>(P, op, v, idx, tm); break;
-            case 1: if constexpr (K >= 2) op_u2<A, K, (K >= 2 ? 1 : 0)>(P, op, v, idx, tm); break;
-            case 2: if constexpr (K >= 3) op_u2<A, K, (K >= 3 ? 2 : 0)>(P, op, v, idx, tm); break;
-            case 3: if constexpr (K >= 4) op_u2<A, K, (K >= 4 ? 3 : 0)>(P, op, v, idx, tm); break;
-          }
+__device__ __forceinline__ void apply_op(const SweepEntry* E, const SweepOp& op, typename A::VT* v,
+                                         const uint64_t* idx, unsigned& tm) {
+  switch (op.kind) {
+    case SW_PHASE:
+      op_phase<A, K>(E, op, v, idx, tm);
+      break;
+    case SW_U2:
+      if constexpr (K >= 1) {
+        switch (op.j0) {
+          case 0: op_u2<A, K, 0>(E, op, v, idx, tm); break;
+          case 1: if constexpr (K >= 2) op_u2<A, K, (K >= 2 ? 1 : 0)>(E, op, v, idx, tm); break;
+          case 2: if constexpr (K >= 3) op_u2<A, K, (K >= 3 ? 2 : 0)>(E, op, v, idx, tm); break;
+          case 3: if constexpr (K >= 4) op_u2<A, K, (K >= 4 ? 3 : 0)>(E, op, v, idx, tm); break;
         }
-        break;
-      case SW_U4:
-      case SW_SWAPLIKE:
-        if constexpr (K >= 2) {
-          const bool u4 = op.kind == SW_U4;
-          const int a = op.j0, b = op.j1;
+      }
+      break;
+    case SW_U4:
+    case SW_SWAPLIKE:
+      if constexpr (K >= 2) {
+        const bool u4 = op.kind == SW_U4;
+        const int a = op.j0, b = op.j1;
 #define IQSG_PAIR_CASE(X, Y)                                                               \
   if (a == X && b == Y) {                                                                  \
     if constexpr (K > (X > Y ? X : Y)) {                                                   \
-      if (u4) op_u4<A, K, X, Y>(P, op, v, idx, tm); else op_swaplike<A, K, X, Y>(P, op, v, idx, tm); \
+      if (u4) op_u4<A, K, X, Y>(E, op, v, idx, tm); else op_swaplike<A, K, X, Y>(E, op, v, idx, tm); \
     }                                                                                      \
   }
-          IQSG_PAIR_CASE(0, 1) IQSG_PAIR_CASE(1, 0) IQSG_PAIR_CASE(0, 2) IQSG_PAIR_CASE(2, 0)
-          IQSG_PAIR_CASE(1, 2) IQSG_PAIR_CASE(2, 1) IQSG_PAIR_CASE(0, 3) IQSG_PAIR_CASE(3, 0)
-          IQSG_PAIR_CASE(1, 3) IQSG_PAIR_CASE(3, 1) IQSG_PAIR_CASE(2, 3) IQSG_PAIR_CASE(3, 2)
+        IQSG_PAIR_CASE(0, 1) IQSG_PAIR_CASE(1, 0) IQSG_PAIR_CASE(0, 2) IQSG_PAIR_CASE(2, 0)
+        IQSG_PAIR_CASE(1, 2) IQSG_PAIR_CASE(2, 1) IQSG_PAIR_CASE(0, 3) IQSG_PAIR_CASE(3, 0)
+        IQSG_PAIR_CASE(1, 3) IQSG_PAIR_CASE(3, 1) IQSG_PAIR_CASE(2, 3) IQSG_PAIR_CASE(3, 2)
 #undef IQSG_PAIR_CASE
-        }
-        break;
+      }
+      break;
+    default:
+      break;
+  }
+}
+
+// Apply every operation of the sweep to one group, in order. Bit s of tm records that slot s
+// was written.
+template <typename A, int K>
+__device__ __forceinline__ void run_ops(const SweepParams& P, typename A::VT* v, const uint64_t* idx, unsigned& tm) {
+#pragma unroll 1
+  for (unsigned o = 0; o < P.nops; ++o) apply_op<A, K>(P.ent, P.ops[o], v, idx, tm);
+}
+
+// ---- adjoint (two-vector) sweeps --------------------------------------------------------
+//
+// The group of psi (v) and the group of lambda (w) are held together. Gate operations act
+// on both; a gradient operation (SW_GRAD1: 2x2 M on active bit j0; SW_GRAD2: 4x4 M on
+// active bits j0 = high, j1 = low; both where (idx & mask) == mask) adds
+// Im sum_x conj(w_x) (M v)_x over the group to accumulator op.value.
+
+template <typename R>
+__device__ __forceinline__ R im_cdot(const typename NativeArith<R>::VT& l, const typename NativeArith<R>::VT& x) {
+  return l.re * x.im - l.im * x.re;
+}
+
+template <typename R, int K, int J>
+__device__ __forceinline__ R grad1(const SweepEntry* E, const SweepOp& op, const typename NativeArith<R>::VT* v,
+                                   const typename NativeArith<R>::VT* w, const uint64_t* idx) {
+  using A = NativeArith<R>;
+  constexpr int G = 1 << K, B = 1 << J;
+  const SweepEntry* m = E + op.ent;
+  R c = 0;
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if (s & B) continue;
+    if ((idx[s] & op.mask) != op.mask) continue;
+    const typename A::VT a = v[s], b = v[s | B];
+    c += im_cdot<R>(w[s], A::row(m[0], m[1], a, b)) + im_cdot<R>(w[s | B], A::row(m[2], m[3], a, b));
+  }
+  return c;
+}
+
+template <typename R, int K, int JH, int JL>
+__device__ __forceinline__ R grad2(const SweepEntry* E, const SweepOp& op, const typename NativeArith<R>::VT* v,
+                                   const typename NativeArith<R>::VT* w, const uint64_t* idx) {
+  using A = NativeArith<R>;
+  constexpr int G = 1 << K, BH = 1 << JH, BL = 1 << JL;
+  const SweepEntry* m = E + op.ent;
+  R c = 0;
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if (s & (BH | BL)) continue;
+    if ((idx[s] & op.mask) != op.mask) continue;
+    const typename A::VT q[4] = {v[s], v[s | BL], v[s | BH], v[s | BH | BL]};
+    c += im_cdot<R>(w[s], A::row4(m, q)) + im_cdot<R>(w[s | BL], A::row4(m + 4, q)) +
+         im_cdot<R>(w[s | BH], A::row4(m + 8, q)) + im_cdot<R>(w[s | BH | BL], A::row4(m + 12, q));
+  }
+  return c;
+}
+
+template <typename R, int K>
+__device__ __forceinline__ R grad_op(const SweepEntry* E, const SweepOp& op, const typename NativeArith<R>::VT* v,
+                                     const typename NativeArith<R>::VT* w, const uint64_t* idx) {
+  if (op.kind == SW_GRAD1) {
+    if constexpr (K >= 1) {
+      switch (op.j0) {
+        case 0: return grad1<R, K, 0>(E, op, v, w, idx);
+        case 1: if constexpr (K >= 2) return grad1<R, K, (K >= 2 ? 1 : 0)>(E, op, v, w, idx); break;
+        case 2: if constexpr (K >= 3) return grad1<R, K, (K >= 3 ? 2 : 0)>(E, op, v, w, idx); break;
+        case 3: if constexpr (K >= 4) return grad1<R, K, (K >= 4 ? 3 : 0)>(E, op, v, w, idx); break;
+      }
+    }
+    return R(0);
+  }
+  if constexpr (K >= 2) {
+    const int a = op.j0, b = op.j1;
+#define IQSG_GRAD_CASE(X, Y)                                         \
+  if (a == X && b == Y) {                                            \
+    if constexpr (K > (X > Y ? X : Y)) return grad2<R, K, X, Y>(E, op, v, w, idx); \
+  }
+    IQSG_GRAD_CASE(0, 1) IQSG_GRAD_CASE(1, 0) IQSG_GRAD_CASE(0, 2) IQSG_GRAD_CASE(2, 0)
+    IQSG_GRAD_CASE(1, 2) IQSG_GRAD_CASE(2, 1) IQSG_GRAD_CASE(0, 3) IQSG_GRAD_CASE(3, 0)
+    IQSG_GRAD_CASE(1, 3) IQSG_GRAD_CASE(3, 1) IQSG_GRAD_CASE(2, 3) IQSG_GRAD_CASE(3, 2)
+#undef IQSG_GRAD_CASE
+  }
+  return R(0);
+}
+
+template <typename R, int K>
+__device__ __forceinline__ void run_ops_dual(const SweepParams& P, typename NativeArith<R>::VT* v,
+                                             typename NativeArith<R>::VT* w, const uint64_t* idx, unsigned& tm,
+                                             R* acc) {
+  using A = NativeArith<R>;
+#pragma unroll 1
+  for (unsigned o = 0; o < P.nops; ++o) {
+    const SweepOp op = P.ops[o];
+    if (op.kind == SW_GRAD1 || op.kind == SW_GRAD2) {
+      acc[op.value] += grad_op<R, K>(P.ent, op, v, w, idx);
+    } else {
+      apply_op<A, K>(P.ent, op, v, idx, tm);
+      apply_op<A, K>(P.ent, op, w, idx, tm);
     }
   }
 }
 
 // Host side: launch one sweep on the register (k_sweep.cu).
 void launch_sweep(iqsg_state* h, const SweepParams& P);
+
+// Host side: one adjoint sweep over psi and lam; gradient slot s adds into grad[param[s]]
+// (a device array of doubles).
+struct GradMap {
+  unsigned nslots;
+  unsigned param[kGradSlots];
+};
+void launch_sweep_adj(iqsg_state* psi, iqsg_state* lam, const SweepParams& P, const GradMap& map, double* grad);
 
 }  // namespace iqsg

@@ -25,7 +25,7 @@ _DP = C.POINTER(C.c_double)
 _UP = C.POINTER(C.c_uint)
 _IP = C.POINTER(C.c_int)
 
-OP_1Q, OP_CTRL, OP_2Q, OP_SWAPLIKE, OP_DIAG2, OP_PHASE = range(6)
+OP_1Q, OP_CTRL, OP_2Q, OP_SWAPLIKE, OP_DIAG2, OP_PHASE, OP_GRAD1, OP_GRAD2 = range(8)
 
 
 class Op(C.Structure):
@@ -83,6 +83,7 @@ SIGNATURES = {
     "iqsg_cost_expectation": [_P, _P, C.c_int, _DP],
     "iqsg_maxcut_cost": [_P, _IP, _UP, _IP],
     "iqsg_apply_ops": [_P, C.POINTER(Op), _U, _UP],
+    "iqsg_adjoint_ops": [_P, _P, C.POINTER(Op), _U, _DP, _U, _UP],
     "iqsg_set_sweep_width": [_P, _U],
     "iqsg_set_option": [_P, C.c_int, C.c_int],
     "iqsg_qaoa_layer": [_P, _U, _UP, _IP, _D, _D],
