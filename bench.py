@@ -315,6 +315,162 @@ def batched_section(count: int = 4096, loop_sample: int = 64) -> dict:
             "max_abs_energy_diff_vs_loop": loop_err}
 
 
+def gate_bytes(ops, n: int, amp_bytes: int) -> int:
+    """Algorithmic bytes of a gate list: 2*N*s per 1-qubit gate, N*s per controlled or
+    swap-type gate (src/highperfkernels.cpp:370, :478-479)."""
+    N = 1 << n
+    one = {"Apply1QubitGate", "ApplyHadamard"}
+    return sum((2 if name in one else 1) * N * amp_bytes for name, _ in ops)
+
+
+def qft_brick_section(n: int = 30, layers: int = 40) -> dict:
+    """QFT + 40 Haar/CZ brick layers from a seeded basis state: ComplexDP gate by gate
+    (emulated arithmetic), ComplexSP in fused passes; errors against the amplitudes the
+    reference itself computed (tests/golden/qft_brick.npz) and SP fidelity against DP."""
+    import hashlib
+    import torch
+    import iqs_gb300 as iqs
+    from circuits import loads, qft_brick, qft_brick_start, replay
+    ops = qft_brick(n, layers)
+    start = qft_brick_start(n)
+    fix = REPO / "tests" / "golden" / "qft_brick.npz"
+    ref = None
+    if fix.exists():  # the stored circuit (a list generated on another machine can differ in the last bit)
+        z = np.load(fix)
+        if f"n{n}/ops" in z.files:
+            meta = json.loads(str(z[f"n{n}/meta"]))
+            text = str(z[f"n{n}/ops"])
+            if meta["layers"] == layers and meta["ops_sha256"] == hashlib.sha256(text.encode()).hexdigest():
+                ops, start = loads(text), meta["start"]
+                ref = (z[f"n{n}/idx"], z[f"n{n}/amps"])
+    out = {"workload": f"{n}-qubit QFT (examples/quantum_fourier_transform.cpp gate order) + {layers} layers of "
+                       f"(Haar U on every qubit + CZ brick), from basis state {start}",
+           "gates": len(ops)}
+
+    def timed(reg, fusion):
+        if fusion:
+            reg.TurnOnFusion()
+        reg.synchronize()
+        t0 = time.perf_counter()
+        replay(reg, ops)
+        sweeps = reg.ApplyFusedGates() if fusion else len(ops)
+        reg.synchronize()
+        return time.perf_counter() - t0, sweeps
+
+    def sample_err(reg):
+        if ref is None:
+            return None
+        v = torch.as_tensor(reg, device="cuda")[torch.as_tensor(ref[0], device="cuda")].cpu().numpy()
+        return float(np.max(np.abs(v.astype(np.complex128) - ref[1])))
+
+    dp = iqs.QubitRegister(n, "base", start, precision="DP", math="emulated")
+    t_dp, _ = timed(dp, False)
+    sp = iqs.QubitRegister(n, "base", start, precision="SP")
+    t_sp, sweeps = timed(sp, True)
+    sp.Initialize("base", start)
+    t_sp, sweeps = timed(sp, True)  # second run: warm
+    a, b = torch.as_tensor(dp, device="cuda"), torch.as_tensor(sp, device="cuda")
+    mx, ov, na, nb = 0.0, 0j, 0.0, 0.0
+    for s0 in range(0, a.numel(), 1 << 26):
+        x, y = a[s0:s0 + (1 << 26)], b[s0:s0 + (1 << 26)].to(torch.complex128)
+        mx = max(mx, float((x - y).abs().max()))
+        ov += complex(torch.vdot(x, y))
+        na += float(torch.vdot(x, x).real)
+        nb += float(torch.vdot(y, y).real)
+    out.update({
+        "dp_gate_by_gate": {"s": round(t_dp, 3), "launches": len(ops),
+                            "gbs_algorithmic": round(gate_bytes(ops, n, 16) / t_dp / 1e9, 1),
+                            "max_abs_err_vs_reference_sample": sample_err(dp)},
+        "sp_fused": {"s": round(t_sp, 3), "passes": sweeps,
+                     "gbs_algorithmic": round(gate_bytes(ops, n, 8) / t_sp / 1e9, 1),
+                     "max_abs_err_vs_reference_sample": sample_err(sp),
+                     "max_abs_diff_vs_dp": mx, "fidelity_vs_dp": abs(ov) ** 2 / (na * nb)},
+        "reference_sample": None if ref is None else f"{ref[0].size} amplitudes from the reference (ComplexDP)",
+    })
+    del a, b, dp, sp
+    torch.cuda.empty_cache()
+    return out
+
+
+def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int = 4) -> dict:
+    """Open XXZ chain (31 bonds at n = 32, J ~ U[0.5, 1.5] seed 7, delta = 0.8, dt = 0.05) from
+    the Neel state: 100 Strang steps in ComplexSP with the 31 bond correlators, then the
+    energy sum_b <Z_b Z_{b+1}> and its gradient w.r.t. every J_b by the checkpointed adjoint;
+    a few steps of the same chain at 33 qubits in ComplexDP (128 GiB) for the HBM roofline;
+    parity of the same 100-step circuit at 20 qubits against the oracle."""
+    import torch
+    import oracle
+    from iqs_gb300 import _lib
+    from iqs_gb300.trotter import XXZChain, bond_gate, strang_layers
+    J = np.random.default_rng(7).uniform(0.5, 1.5, n - 1)
+    out = {"workload": f"open XXZ chain, {n} qubits ComplexSP, delta 0.8, dt 0.05, {steps} Strang steps "
+                       f"(even half steps merged), Neel start; bond gate = RXX RYY RZZ as one 2-qubit gate"}
+    vec = (1 << n) * 8
+    free = torch.cuda.mem_get_info()[0]
+    every = None
+    for c in (10, 20, 25, 50):
+        if (2 + len(range(c, steps, c))) * vec + (16 << 30) <= free:
+            every = c
+            break
+    chain = XXZChain(n, J, steps=steps, precision="SP", checkpoint_every=every)
+    gates = sum(len(b) for b, _ in chain.layers())
+    chain.psi.synchronize()
+    t0 = time.perf_counter()
+    zz = chain.bond_zz()
+    chain.psi.synchronize()
+    t_fwd = time.perf_counter() - t0
+    fwd_sweeps = chain.sweeps_forward
+    chain.sweeps_forward = 0
+    t0 = time.perf_counter()
+    e, grad = chain.energy_and_grad()
+    t_grad = time.perf_counter() - t0
+    N = 1 << n
+    out["sp"] = {"gates": gates, "forward_s": round(t_fwd, 3), "forward_passes": fwd_sweeps,
+                 "forward_gbs_algorithmic": round(gates * 2 * N * 8 / t_fwd / 1e9, 1),
+                 "forward_pass_gbs": round(fwd_sweeps * 2 * N * 8 / t_fwd / 1e9, 1),
+                 "zz_first4": [round(float(x), 8) for x in zz[:4]], "zz_mean": float(np.mean(zz)),
+                 "energy": e, "energy_minus_sum_zz": float(e - np.sum(zz)),
+                 "grad_first4": [round(float(x), 8) for x in grad[:4]], "grad_norm": float(np.linalg.norm(grad)),
+                 "forward_and_grad_s": round(t_grad, 3), "adjoint_passes": chain.sweeps_backward,
+                 "checkpoint_every_steps": every, "checkpoints": len(chain._ckpt)}
+    del chain
+    # 33-qubit ComplexDP forward, emulated arithmetic: roofline of the fused passes.
+    Jd = np.random.default_rng(7).uniform(0.5, 1.5, n_dp - 1)
+    if (1 << n_dp) * 16 + (8 << 30) <= torch.cuda.mem_get_info()[0]:
+        ch = XXZChain(n_dp, Jd, steps=steps_dp, precision="DP", checkpoint_every=None)
+        ch.psi.SetMath("emulated")
+        ch.forward()
+        ch.psi.synchronize()
+        ch.sweeps_forward = 0
+        t0 = time.perf_counter()
+        ch.forward()
+        ch.psi.synchronize()
+        t = time.perf_counter() - t0
+        gd = sum(len(b) for b, _ in ch.layers())
+        out["dp33"] = {"qubits": n_dp, "steps": steps_dp, "gates": gd, "passes": ch.sweeps_forward, "s": round(t, 3),
+                       "gbs_algorithmic": round(gd * 2 * (1 << n_dp) * 16 / t / 1e9, 1),
+                       "pass_gbs": round(ch.sweeps_forward * 2 * (1 << n_dp) * 16 / t / 1e9, 1),
+                       "math": "emulated"}
+        del ch
+    # parity: the same 100-step circuit at 20 qubits, SP and DP, against the oracle
+    n20 = 20
+    J20 = np.random.default_rng(7).uniform(0.5, 1.5, n20 - 1)
+    o = oracle.OracleRegister(n20, "base", sum(1 << q for q in range(1, n20, 2)))
+    for bonds, tau in strang_layers(n20, 0.05, steps):
+        for b in bonds:
+            o.Apply2QubitGate(b + 1, b, bond_gate(0.5 * tau * J20[b], 0.8))
+    want = np.asarray([o.ExpectationValue([b, b + 1], [3, 3], 1.0) for b in range(n20 - 1)])
+    ost = o.GetStateVector()
+    par = {}
+    for prec in ("DP", "SP"):
+        c20 = XXZChain(n20, J20, steps=steps, precision=prec, checkpoint_every=None)
+        z20 = c20.bond_zz()
+        par[prec] = {"max_abs_zz_err": float(np.max(np.abs(z20 - want))),
+                     "max_abs_amp_err": float(np.max(np.abs(c20.psi.GetStateVector() - ost)))}
+    out["parity_20q_vs_oracle"] = par
+    return out
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -449,6 +605,8 @@ def run_ours(args) -> None:
     cpu = None
     qaoa = None
     batched = None
+    qft = None
+    trotter = None
     if rank == 0:
         import oracle
         oracle.build(ref=False)
@@ -469,6 +627,8 @@ def run_ours(args) -> None:
             cpu = cpu_layer_gbs(args.cpu_qubits, 1, seed=5, threads=threads)
         qaoa = None if args.no_adjoint else qaoa_section(stream=stream.cuda_stream)
         batched = None if args.no_batched else batched_section()
+        qft = None if args.no_qft else qft_brick_section()
+        trotter = None if args.no_trotter else trotter_section()
 
     if rank == 0:
         dtype = "c128: f64 storage, double-float (fp32x2) products and sums" if args.math == "emulated" else "f64"
@@ -502,6 +662,10 @@ def run_ours(args) -> None:
             line["adjoint"] = qaoa
         if batched is not None:
             line["batched"] = batched
+        if qft is not None:
+            line["qft_brick"] = qft
+        if trotter is not None:
+            line["trotter"] = trotter
         if cpu is not None:
             line["cpu_baseline"] = {"value": round(cpu["gbs"], 3), "unit": UNIT, "cores": cpu["cores"],
                                     "kind": cpu["kind"],
@@ -530,6 +694,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the QAOA adjoint-gradient section")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-circuits section")
+    ap.add_argument("--no-qft", action="store_true", help="skip the QFT + brick-layers section")
+    ap.add_argument("--no-trotter", action="store_true", help="skip the XXZ Trotter section")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per 1-qubit-gate launch from an ncu capture, if known")
     args = ap.parse_args()

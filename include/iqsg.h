@@ -220,9 +220,16 @@ int iqsg_set_sweep_width(iqsg_state* h, unsigned kmax);
 /* Tuning options of a register (iqsg_set_option). */
 typedef enum {
   IQSG_OPT_SWEEP_WIDTH = 0,    /* same as iqsg_set_sweep_width */
-  IQSG_OPT_SWEEP_PIPELINE = 1  /* 1: fused passes on registers of 16+ qubits stream tiles through
+  IQSG_OPT_SWEEP_PIPELINE = 1, /* 1: fused passes on registers of 16+ qubits stream tiles through
                                   shared memory with bulk async copies; 0 (default): each thread
                                   loads its groups directly */
+  IQSG_OPT_TILE_QUBITS = 2     /* k > 0: run gate streams (iqsg_apply_ops, iqsg_adjoint_ops) as
+                                  tile passes: each pass stages tiles spanning k positions (the
+                                  lowest 3 or 4 included; at most 14 for ComplexSP, 13 for
+                                  ComplexDP, one less for adjoint passes) in shared memory and
+                                  applies every gate of a stretch of the stream that acts inside
+                                  them, gates on disjoint positions reordered; 0 (default): register
+                                  sweeps only. Not used for emulated ComplexDP arithmetic. */
 } iqsg_option;
 
 /* Set a tuning option; results never depend on it. */

@@ -21,6 +21,7 @@ struct iqsg_state {
   void* tmp = nullptr;            // device: out-of-place permutation buffer (lazy)
   size_t tmp_bytes = 0;
   unsigned sweep_width = 0;       // fused-sweep width limit (0 = default for the precision)
+  unsigned tile_qubits = 0;       // positions per shared-memory tile pass (0 = register sweeps only)
   bool bulk = false;              // fused passes through the bulk-copy pipeline (IQSG_OPT_SWEEP_PIPELINE)
 };
 
@@ -141,5 +142,10 @@ void launch_1q_emulated(iqsg_state* h, unsigned pos, const M2<double>& m);
 
 // ---- fused sweeps (k_sweep.cu) ----
 unsigned sweep_width(const iqsg_state* h);
+// Tile passes (k_tile.cu): the tile size in positions for this register (0 = not used), and
+// the scheduler that runs validated ops as tile passes (lam != NULL: adjoint passes).
+unsigned tile_qubits(const iqsg_state* h, bool dual);
+int tile_schedule(iqsg_state* h, iqsg_state* lam, const iqsg_op* ops, unsigned count, unsigned kt, unsigned kmax,
+                  double* grad, unsigned* passes);
 
 }  // namespace iqsg

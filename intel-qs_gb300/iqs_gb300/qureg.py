@@ -293,6 +293,13 @@ class QubitRegister:
         self._flush()
         check(lib.iqsg_set_sweep_width(self._h, int(kmax)))
 
+    def SetTileQubits(self, k: int) -> None:
+        """Run fused gate streams as shared-memory tile passes spanning k positions (0 = off,
+        register sweeps only); a tuning choice that changes results only by rounding (gates
+        on disjoint qubits may be applied in a different order)."""
+        self._flush()
+        check(lib.iqsg_set_option(self._h, _lib.OPT_TILE_QUBITS, int(k)))
+
     def SetSweepPipeline(self, on: bool) -> None:
         """Stream fused passes through shared memory with bulk async copies (registers of 16+
         qubits); a tuning choice that never changes results."""

@@ -74,7 +74,7 @@ def _op4(kind: int, hi: int, lo: int, m: np.ndarray, value: int = 0) -> _lib.Op:
 class XXZChain:
     def __init__(self, num_qubits: int, J: Sequence[float], *, delta: float = 0.8, dt: float = 0.05, steps: int = 100,
                  precision: str = "SP", checkpoint_every: Optional[int] = 10, weights: Optional[Sequence[int]] = None,
-                 stream: Optional[int] = None):
+                 stream: Optional[int] = None, tile_qubits: int = 0):
         self.n = int(num_qubits)
         if len(J) != self.n - 1:
             raise ValueError(f"expected {self.n - 1} couplings, got {len(J)}")
@@ -83,7 +83,9 @@ class XXZChain:
         self.precision, self.stream = precision, stream
         self.checkpoint_every = checkpoint_every
         self.weights = np.ones(self.n - 1, dtype=np.int32) if weights is None else np.asarray(weights, dtype=np.int32)
+        self.tile_qubits = int(tile_qubits)
         self.psi = QubitRegister(self.n, "", 0, precision=precision, stream=stream)
+        self.psi.SetTileQubits(self.tile_qubits)
         self.lam: Optional[QubitRegister] = None
         self._ckpt: List[QubitRegister] = []
         self.sweeps_forward = 0

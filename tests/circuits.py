@@ -172,6 +172,41 @@ def plain_gate_by_gate(n: int = 20, layers: int = 20, seed: int = 1) -> List[lis
     return ops
 
 
+def qft_ops(n: int) -> List[list]:
+    """Quantum Fourier transform in the gate order of examples/quantum_fourier_transform.cpp:49-71:
+    for i = n-1..0, controlled phase diag(1, e^{i pi / 2^(j-i)}) with control j > i (from n-1
+    down) on target i, then H(i); then SWAP(i, n-1-i) for i < n/2."""
+    ops: List[list] = []
+    for i in range(n - 1, -1, -1):
+        for j in range(n - 1, i, -1):
+            ph = math.pi / float(1 << (j - i))
+            ops.append(["ApplyControlled1QubitGate", [j, i, enc([[1, 0], [0, complex(math.cos(ph), math.sin(ph))]])]])
+        ops.append(["ApplyHadamard", [i]])
+    for i in range(n // 2):
+        ops.append(["ApplySwap", [i, n - 1 - i]])
+    return ops
+
+
+def qft_brick(n: int = 30, layers: int = 40, seed: int = 2) -> List[list]:
+    """QFT followed by `layers` layers of (Haar U on every qubit + CZ brick, even then odd)."""
+    rng = np.random.default_rng(seed)
+    ops = qft_ops(n)
+    for _ in range(layers):
+        ops += brick_layer_ops(n, rng, "ApplyCPauliZ")
+    return ops
+
+
+def qft_brick_start(n: int, seed: int = 2) -> int:
+    """Basis state the QFT + brick circuit starts from (a QFT of |0...0> would be trivial)."""
+    return int(np.random.default_rng(seed + 1000).integers(1 << n))
+
+
+def qft_brick_queries(n: int) -> List[list]:
+    """Queries read after the QFT + brick circuit."""
+    return [["ComputeNorm", []], ["GetProbability", [0]], ["GetProbability", [n - 1]],
+            ["ExpectationValue", [[0, n - 1], [3, 3], 1.0]]]
+
+
 def dumps(ops) -> str:
     return json.dumps(ops, separators=(",", ":"))
 
