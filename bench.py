@@ -392,12 +392,13 @@ def qft_brick_section(n: int = 30, layers: int = 40) -> dict:
     return out
 
 
-def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int = 4) -> dict:
+def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int = 4, grad_steps: int = 10) -> dict:
     """Open XXZ chain (31 bonds at n = 32, J ~ U[0.5, 1.5] seed 7, delta = 0.8, dt = 0.05) from
     the Neel state: 100 Strang steps in ComplexSP with the 31 bond correlators, then the
     energy sum_b <Z_b Z_{b+1}> and its gradient w.r.t. every J_b by the checkpointed adjoint;
     a few steps of the same chain at 33 qubits in ComplexDP (128 GiB) for the HBM roofline;
-    parity of the same 100-step circuit at 20 qubits against the oracle."""
+    parity of the same 100-step circuit at 20 qubits against the oracle. The gradient runs
+    over the first `grad_steps` Strang steps (all of them with grad_steps = steps)."""
     import torch
     import oracle
     from iqs_gb300 import _lib
@@ -412,7 +413,7 @@ def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int
         if (2 + len(range(c, steps, c))) * vec + (16 << 30) <= free:
             every = c
             break
-    chain = XXZChain(n, J, steps=steps, precision="SP", checkpoint_every=every)
+    chain = XXZChain(n, J, steps=steps, precision="SP", checkpoint_every=None)
     gates = sum(len(b) for b, _ in chain.layers())
     chain.psi.synchronize()
     t0 = time.perf_counter()
@@ -421,19 +422,27 @@ def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int
     t_fwd = time.perf_counter() - t0
     fwd_sweeps = chain.sweeps_forward
     chain.sweeps_forward = 0
+    del chain
+    gchain = XXZChain(n, J, steps=grad_steps, precision="SP",
+                      checkpoint_every=every if (every and grad_steps > every) else None)
+    gchain.forward()
+    gchain.psi.synchronize()
     t0 = time.perf_counter()
-    e, grad = chain.energy_and_grad()
+    e, grad = gchain.energy_and_grad()
     t_grad = time.perf_counter() - t0
     N = 1 << n
     out["sp"] = {"gates": gates, "forward_s": round(t_fwd, 3), "forward_passes": fwd_sweeps,
                  "forward_gbs_algorithmic": round(gates * 2 * N * 8 / t_fwd / 1e9, 1),
                  "forward_pass_gbs": round(fwd_sweeps * 2 * N * 8 / t_fwd / 1e9, 1),
                  "zz_first4": [round(float(x), 8) for x in zz[:4]], "zz_mean": float(np.mean(zz)),
-                 "energy": e, "energy_minus_sum_zz": float(e - np.sum(zz)),
-                 "grad_first4": [round(float(x), 8) for x in grad[:4]], "grad_norm": float(np.linalg.norm(grad)),
-                 "forward_and_grad_s": round(t_grad, 3), "adjoint_passes": chain.sweeps_backward,
-                 "checkpoint_every_steps": every, "checkpoints": len(chain._ckpt)}
-    del chain
+                 "gradient": {"strang_steps": grad_steps, "energy": e,
+                              "grad_first4": [round(float(x), 8) for x in grad[:4]],
+                              "grad_norm": float(np.linalg.norm(grad)),
+                              "forward_and_grad_s": round(t_grad, 3), "adjoint_passes": gchain.sweeps_backward,
+                              "adjoint_pass_gbs": round(gchain.sweeps_backward * 4 * N * 8 /
+                                                        max(t_grad - t_fwd * grad_steps / steps, 1e-9) / 1e9, 1),
+                              "checkpoint_every_steps": gchain.checkpoint_every, "checkpoints": len(gchain._ckpt)}}
+    del gchain
     # 33-qubit ComplexDP forward, emulated arithmetic: roofline of the fused passes.
     Jd = np.random.default_rng(7).uniform(0.5, 1.5, n_dp - 1)
     if (1 << n_dp) * 16 + (8 << 30) <= torch.cuda.mem_get_info()[0]:
@@ -503,6 +512,8 @@ def run_ours(args) -> None:
     if args.width:
         reg.SetSweepWidth(args.width)
         reg.SetSweepPipeline(args.pipeline)
+        if args.math == "emulated":
+            reg.SetNativeShare(args.native_share)
     elif args.fusion:
         from iqs_gb300.autotune import tune_fusion
         tuned = tune_fusion(reg)  # untimed: picks the pass width and kernel for this register
@@ -628,7 +639,7 @@ def run_ours(args) -> None:
         qaoa = None if args.no_adjoint else qaoa_section(stream=stream.cuda_stream)
         batched = None if args.no_batched else batched_section()
         qft = None if args.no_qft else qft_brick_section()
-        trotter = None if args.no_trotter else trotter_section()
+        trotter = None if args.no_trotter else trotter_section(grad_steps=100 if args.full_trotter else 10)
 
     if rank == 0:
         dtype = "c128: f64 storage, double-float (fp32x2) products and sums" if args.math == "emulated" else "f64"
@@ -642,7 +653,10 @@ def run_ours(args) -> None:
                        "math": args.math, "fusion": bool(args.fusion),
                        "sweep_width": args.width or (tuned["width"] if tuned else "default"),
                        "sweep_pipeline": bool(args.pipeline if args.width else (tuned["pipeline"] if tuned else False)),
-                       "autotune_ms": [[r["width"], r["pipeline"], round(r["ms"], 1)] for r in tuned["table"]] if tuned else None,
+                       "native_share_16ths": (args.native_share if args.width else (tuned["native_share"] if tuned else 0))
+                       if args.math == "emulated" else None,
+                       "autotune_ms": [[r["width"], r["pipeline"], r["native_share"], round(r["ms"], 1)]
+                                       for r in tuned["table"]] if tuned else None,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "state (16 GiB) far larger than L2 (129 MB); no flush needed"},
             "roofline": {"bound": "hbm", "kernel": kname,
@@ -691,11 +705,15 @@ def main() -> None:
     ap.add_argument("--width", type=int, default=0,
                     help="fused-pass width (target qubits per pass); 0 = chosen by the autotuner")
     ap.add_argument("--pipeline", type=int, default=0, help="with --width: 1 = bulk-copy pipelined passes")
+    ap.add_argument("--native-share", type=int, default=0,
+                    help="with --width and emulated math: sixteenths of the warps on native FP64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the QAOA adjoint-gradient section")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-circuits section")
     ap.add_argument("--no-qft", action="store_true", help="skip the QFT + brick-layers section")
     ap.add_argument("--no-trotter", action="store_true", help="skip the XXZ Trotter section")
+    ap.add_argument("--full-trotter", action="store_true",
+                    help="adjoint gradient over all 100 Strang steps at 32 qubits (about 1.5 min more)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per 1-qubit-gate launch from an ncu capture, if known")
     args = ap.parse_args()

@@ -223,16 +223,21 @@ typedef enum {
   IQSG_OPT_SWEEP_PIPELINE = 1, /* 1: fused passes on registers of 16+ qubits stream tiles through
                                   shared memory with bulk async copies; 0 (default): each thread
                                   loads its groups directly */
-  IQSG_OPT_TILE_QUBITS = 2     /* k > 0: run gate streams (iqsg_apply_ops, iqsg_adjoint_ops) as
+  IQSG_OPT_TILE_QUBITS = 2,    /* k > 0: run gate streams (iqsg_apply_ops, iqsg_adjoint_ops) as
                                   tile passes: each pass stages tiles spanning k positions (the
                                   lowest 3 or 4 included; at most 14 for ComplexSP, 13 for
                                   ComplexDP, one less for adjoint passes) in shared memory and
                                   applies every gate of a stretch of the stream that acts inside
                                   them, gates on disjoint positions reordered; 0 (default): register
                                   sweeps only. Not used for emulated ComplexDP arithmetic. */
+  IQSG_OPT_NATIVE_SHARE = 3    /* s in 0..16: in emulated-ComplexDP fused sweeps, s/16 of the warps
+                                  apply their groups in native FP64 (the FP64 pipe) while the rest
+                                  use double-float FP32 arithmetic; 0 (default): all emulated.
+                                  Results differ from s = 0 only by rounding. */
 } iqsg_option;
 
-/* Set a tuning option; results never depend on it. */
+/* Set a tuning option. Results depend on it at most by rounding (tile passes reorder gates on
+ * disjoint positions; the native share changes which arithmetic a group gets). */
 int iqsg_set_option(iqsg_state* h, int option, int value);
 
 /* ---- reductions (FP64 accumulation; each waits for its result) ------------------------ */

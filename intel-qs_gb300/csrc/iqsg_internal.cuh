@@ -23,6 +23,7 @@ struct iqsg_state {
   unsigned sweep_width = 0;       // fused-sweep width limit (0 = default for the precision)
   unsigned tile_qubits = 0;       // positions per shared-memory tile pass (0 = register sweeps only)
   bool bulk = false;              // fused passes through the bulk-copy pipeline (IQSG_OPT_SWEEP_PIPELINE)
+  unsigned native16 = 0;          // emulated ComplexDP sweeps: share (in 16ths) of warps on the FP64 pipe
 };
 
 namespace iqsg {

@@ -59,7 +59,9 @@ __global__ void __launch_bounds__(kThreads) k_sweep_native(typename V2<R>::type*
 }
 
 // FP64 storage, double-float arithmetic; a group with a value outside the fast range is
-// recomputed in native FP64. Untouched slots are not rewritten.
+// recomputed in native FP64. Untouched slots are not rewritten. With P.native16 > 0, whole
+// warps (a fixed share of the group blocks) take the native FP64 path from the start, so the
+// FP64 pipe works alongside the FP32 pipes that carry the double-float arithmetic.
 template <int K>
 __global__ void __launch_bounds__(kThreads) k_sweep_df(double2* __restrict__ s, uint64_t ngroups,
                                                        const __grid_constant__ SweepParams P) {
@@ -71,11 +73,13 @@ __global__ void __launch_bounds__(kThreads) k_sweep_df(double2* __restrict__ s, 
 #pragma unroll
     for (int k = 0; k < G; ++k) raw[k] = s[idx[k]];
     DF64Arith::VT v[G];
-    bool ok = true;
+    bool ok = ((g >> 5) & 15) >= P.native16;  // warp-uniform: gstride and the block size are multiples of 32
+    if (ok) {
 #pragma unroll
-    for (int k = 0; k < G; ++k) {
-      ok &= df64::split(raw[k].x, v[k].re);
-      ok &= df64::split(raw[k].y, v[k].im);
+      for (int k = 0; k < G; ++k) {
+        ok &= df64::split(raw[k].x, v[k].re);
+        ok &= df64::split(raw[k].y, v[k].im);
+      }
     }
     unsigned tm = 0;
     double2 out[G];
@@ -514,6 +518,10 @@ extern "C" int iqsg_set_option(iqsg_state* h, int option, int value) {
       return iqsg_set_sweep_width(h, (unsigned)value);
     case IQSG_OPT_SWEEP_PIPELINE:
       h->bulk = value != 0;
+      return IQSG_OK;
+    case IQSG_OPT_NATIVE_SHARE:
+      if (value < 0 || value > 16) return fail(IQSG_EINVAL, "iqsg_set_option: native share %d outside 0..16", value);
+      h->native16 = (unsigned)value;
       return IQSG_OK;
     case IQSG_OPT_TILE_QUBITS:
       if (value < 0 || value > 14) return fail(IQSG_EINVAL, "iqsg_set_option: tile size %d outside 0..14", value);

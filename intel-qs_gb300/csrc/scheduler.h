@@ -138,21 +138,16 @@ class SweepBuilder {
       return;
     }
     if (excitation) {
-      // Phases on |00> and |11>, a 2x2 on {|01>, |10>} (rows/columns 1 = low bit set, 2 = high bit set).
-      add_phase(bh | bl, 0, m[0], m[1]);
-      add_phase(bh | bl, bh | bl, m[30], m[31]);
-      auto e = [&](int r, int c, double* o) {
-        o[0] = m[2 * (4 * r + c)];
-        o[1] = m[2 * (4 * r + c) + 1];
-      };
-      double w[8];
-      // add_swaplike orders the pair as (lower position set, higher position set).
-      const int a = pl < ph ? 1 : 2, b = pl < ph ? 2 : 1;
-      e(a, a, w);
-      e(a, b, w + 2);
-      e(b, a, w + 4);
-      e(b, b, w + 6);
-      add_swaplike(pl, ph, w);
+      double w[12];
+      excitation_entries(ph, pl, m, w);
+      const unsigned lo = std::min(ph, pl), hi = std::max(ph, pl);
+      reserve({lo, hi}, 1, 6);
+      SweepOp op{};
+      op.kind = SW_EXC;
+      op.j0 = (uint8_t)slot(lo);
+      op.j1 = (uint8_t)slot(hi);
+      op.ent = add_entries(w, 6);
+      P_.ops[P_.nops++] = op;
       return;
     }
     reserve({ph, pl}, 1, 16);
@@ -162,6 +157,30 @@ class SweepBuilder {
     op.j1 = (uint8_t)slot(pl);
     op.ent = add_entries(m, 16);
     P_.ops[P_.nops++] = op;
+  }
+
+  // A 4x4 (rows 2*b(ph) + b(pl)) that maps |01> and |10> into each other and only scales
+  // |00> and |11>, as the six SW_EXC entries (pair ordered lower position first).
+  static bool is_excitation(const double* m) {
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) {
+        const bool inner = (r == 1 || r == 2) && (c == 1 || c == 2);
+        if (r != c && !inner && !is_zero(m[2 * (4 * r + c)], m[2 * (4 * r + c) + 1])) return false;
+      }
+    return true;
+  }
+  static void excitation_entries(unsigned ph, unsigned pl, const double* m, double* w) {
+    auto e = [&](int r, int c, double* o) {
+      o[0] = m[2 * (4 * r + c)];
+      o[1] = m[2 * (4 * r + c) + 1];
+    };
+    const int a = pl < ph ? 1 : 2, b = pl < ph ? 2 : 1;  // row of (lower set), row of (higher set)
+    e(0, 0, w);
+    e(a, a, w + 2);
+    e(a, b, w + 4);
+    e(b, a, w + 6);
+    e(b, b, w + 8);
+    e(3, 3, w + 10);
   }
 
   void add_swaplike(unsigned p1, unsigned p2, const double* m) {
@@ -179,6 +198,21 @@ class SweepBuilder {
   // Adjoint mode: add Im <lam|M|psi> on the target positions into grad[param]; M is 2x2
   // (one target) or 4x4 (rows 2*b(t0) + b(t1)).
   void add_grad(unsigned ntargets, unsigned t0, unsigned t1, const double* m, unsigned param) {
+    if (ntargets == 2 && is_excitation(m)) {
+      double w[12];
+      excitation_entries(t0, t1, m, w);
+      const unsigned lo = std::min(t0, t1), hi = std::max(t0, t1);
+      reserve({lo, hi}, 1, 6, 1);
+      SweepOp op{};
+      op.kind = SW_GRADEXC;
+      op.j0 = (uint8_t)slot(lo);
+      op.j1 = (uint8_t)slot(hi);
+      op.value = map_.nslots;
+      map_.param[map_.nslots++] = param;
+      op.ent = add_entries(w, 6);
+      P_.ops[P_.nops++] = op;
+      return;
+    }
     const unsigned ne = ntargets == 1 ? 4u : 16u;
     if (ntargets == 1) reserve({t0}, 1, ne, 1);
     else reserve({t0, t1}, 1, ne, 1);
@@ -196,6 +230,7 @@ class SweepBuilder {
     if (P_.nops) {
       std::copy(P_.pos, P_.pos + P_.K, P_.sorted);
       std::sort(P_.sorted, P_.sorted + P_.K);
+      P_.native16 = h_ ? h_->native16 : 0u;
       if (sink_) sink_->take(P_, map_);
       else if (lam_) launch_sweep_adj(h_, lam_, P_, map_, grad_);
       else launch_sweep(h_, P_);

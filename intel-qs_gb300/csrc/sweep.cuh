@@ -28,6 +28,10 @@ enum SweepKind : uint8_t {
   SW_SWAPLIKE = 3,  // 2x2 on the (j0 = 1, j1 = 0) / (j0 = 0, j1 = 1) pair, where (idx & mask) == mask
   SW_GRAD1 = 4,     // adjoint sweeps only: accumulate Im <w|M|v>, M 2x2 on j0
   SW_GRAD2 = 5,     // adjoint sweeps only: accumulate Im <w|M|v>, M 4x4 on (j0 high, j1 low)
+  SW_EXC = 6,       // excitation-preserving 4x4 on (j0 = lower, j1 = higher position): entry 0
+                    // scales |00>, entries 1-4 are the 2x2 on (|lo=1,hi=0>, |lo=0,hi=1>), entry 5
+                    // scales |11>; where (idx & mask) == mask
+  SW_GRADEXC = 7,   // adjoint sweeps only: Im <w|M|v> for M with the SW_EXC layout
 };
 
 enum SweepFlags : uint8_t {
@@ -58,6 +62,7 @@ struct SweepParams {
   unsigned pos[kSweepMaxK];     // active slot bit j <-> position pos[j]
   unsigned sorted[kSweepMaxK];  // active positions ascending (zero insertion)
   unsigned nops;
+  unsigned native16;  // emulated FP64 sweeps: warps whose group block (g / 32) % 16 < native16 use FP64
   SweepOp ops[kSweepMaxOps];
   SweepEntry ent[kSweepMaxEntries];
 };
@@ -253,6 +258,24 @@ __device__ __forceinline__ void op_swaplike(const SweepEntry* E, const SweepOp& 
   }
 }
 
+template <typename A, int K, int JLO, int JHI>
+__device__ __forceinline__ void op_exc(const SweepEntry* E, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
+                                       unsigned& tm) {
+  constexpr int G = 1 << K, BL = 1 << JLO, BH = 1 << JHI;
+  const SweepEntry* m = E + op.ent;
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if (s & (BH | BL)) continue;
+    if ((idx[s] & op.mask) != op.mask) continue;
+    tm |= (1u << s) | (1u << (s | BL)) | (1u << (s | BH)) | (1u << (s | BH | BL));
+    const typename A::VT a = v[s | BL], b = v[s | BH];
+    v[s] = A::mul(m[0], v[s]);
+    v[s | BL] = A::row(m[1], m[2], a, b);
+    v[s | BH] = A::row(m[3], m[4], a, b);
+    v[s | BH | BL] = A::mul(m[5], v[s | BH | BL]);
+  }
+}
+
 template <typename A, int K>
 __device__ __forceinline__ void op_phase(const SweepEntry* E, const SweepOp& op, typename A::VT* v, const uint64_t* idx,
                                          unsigned& tm) {
@@ -290,13 +313,16 @@ __device__ __forceinline__ void apply_op(const SweepEntry* E, const SweepOp& op,
       break;
     case SW_U4:
     case SW_SWAPLIKE:
+    case SW_EXC:
       if constexpr (K >= 2) {
-        const bool u4 = op.kind == SW_U4;
+        const int kind = op.kind;
         const int a = op.j0, b = op.j1;
 #define IQSG_PAIR_CASE(X, Y)                                                               \
   if (a == X && b == Y) {                                                                  \
     if constexpr (K > (X > Y ? X : Y)) {                                                   \
-      if (u4) op_u4<A, K, X, Y>(E, op, v, idx, tm); else op_swaplike<A, K, X, Y>(E, op, v, idx, tm); \
+      if (kind == SW_U4) op_u4<A, K, X, Y>(E, op, v, idx, tm);                             \
+      else if (kind == SW_SWAPLIKE) op_swaplike<A, K, X, Y>(E, op, v, idx, tm);            \
+      else op_exc<A, K, X, Y>(E, op, v, idx, tm);                                          \
     }                                                                                      \
   }
         IQSG_PAIR_CASE(0, 1) IQSG_PAIR_CASE(1, 0) IQSG_PAIR_CASE(0, 2) IQSG_PAIR_CASE(2, 0)
@@ -365,6 +391,24 @@ __device__ __forceinline__ R grad2(const SweepEntry* E, const SweepOp& op, const
   return c;
 }
 
+template <typename R, int K, int JLO, int JHI>
+__device__ __forceinline__ R grad_exc(const SweepEntry* E, const SweepOp& op, const typename NativeArith<R>::VT* v,
+                                      const typename NativeArith<R>::VT* w, const uint64_t* idx) {
+  using A = NativeArith<R>;
+  constexpr int G = 1 << K, BL = 1 << JLO, BH = 1 << JHI;
+  const SweepEntry* m = E + op.ent;
+  R c = 0;
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if (s & (BH | BL)) continue;
+    if ((idx[s] & op.mask) != op.mask) continue;
+    const typename A::VT a = v[s | BL], b = v[s | BH];
+    c += im_cdot<R>(w[s], A::mul(m[0], v[s])) + im_cdot<R>(w[s | BL], A::row(m[1], m[2], a, b)) +
+         im_cdot<R>(w[s | BH], A::row(m[3], m[4], a, b)) + im_cdot<R>(w[s | BH | BL], A::mul(m[5], v[s | BH | BL]));
+  }
+  return c;
+}
+
 template <typename R, int K>
 __device__ __forceinline__ R grad_op(const SweepEntry* E, const SweepOp& op, const typename NativeArith<R>::VT* v,
                                      const typename NativeArith<R>::VT* w, const uint64_t* idx) {
@@ -381,9 +425,10 @@ __device__ __forceinline__ R grad_op(const SweepEntry* E, const SweepOp& op, con
   }
   if constexpr (K >= 2) {
     const int a = op.j0, b = op.j1;
+    const bool exc = op.kind == SW_GRADEXC;
 #define IQSG_GRAD_CASE(X, Y)                                         \
   if (a == X && b == Y) {                                            \
-    if constexpr (K > (X > Y ? X : Y)) return grad2<R, K, X, Y>(E, op, v, w, idx); \
+    if constexpr (K > (X > Y ? X : Y)) return exc ? grad_exc<R, K, X, Y>(E, op, v, w, idx) : grad2<R, K, X, Y>(E, op, v, w, idx); \
   }
     IQSG_GRAD_CASE(0, 1) IQSG_GRAD_CASE(1, 0) IQSG_GRAD_CASE(0, 2) IQSG_GRAD_CASE(2, 0)
     IQSG_GRAD_CASE(1, 2) IQSG_GRAD_CASE(2, 1) IQSG_GRAD_CASE(0, 3) IQSG_GRAD_CASE(3, 0)
@@ -401,7 +446,7 @@ __device__ __forceinline__ void run_ops_dual(const SweepParams& P, typename Nati
 #pragma unroll 1
   for (unsigned o = 0; o < P.nops; ++o) {
     const SweepOp op = P.ops[o];
-    if (op.kind == SW_GRAD1 || op.kind == SW_GRAD2) {
+    if (op.kind == SW_GRAD1 || op.kind == SW_GRAD2 || op.kind == SW_GRADEXC) {
       acc[op.value] += grad_op<R, K>(P.ent, op, v, w, idx);
     } else {
       apply_op<A, K>(P.ent, op, v, idx, tm);

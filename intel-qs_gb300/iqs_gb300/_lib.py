@@ -15,7 +15,7 @@ LIB_PATH = _HERE / "libiqsg.so"
 IQSG_OK, IQSG_EINVAL, IQSG_ENOMEM, IQSG_EDEVICE, IQSG_ETIMEOUT, IQSG_ENOTSUP = range(6)
 COMPLEX_DP, COMPLEX_SP = 0, 1
 MATH_NATIVE, MATH_EMULATED = 0, 1
-OPT_SWEEP_WIDTH, OPT_SWEEP_PIPELINE, OPT_TILE_QUBITS = 0, 1, 2
+OPT_SWEEP_WIDTH, OPT_SWEEP_PIPELINE, OPT_TILE_QUBITS, OPT_NATIVE_SHARE = 0, 1, 2, 3
 
 _P = C.c_void_p
 _U = C.c_uint

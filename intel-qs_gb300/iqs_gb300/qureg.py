@@ -293,6 +293,12 @@ class QubitRegister:
         self._flush()
         check(lib.iqsg_set_sweep_width(self._h, int(kmax)))
 
+    def SetNativeShare(self, sixteenths: int) -> None:
+        """Emulated ComplexDP fused sweeps: let sixteenths/16 of the warps use native FP64 (the
+        FP64 pipe runs alongside the FP32 pipes); results change only by rounding."""
+        self._flush()
+        check(lib.iqsg_set_option(self._h, _lib.OPT_NATIVE_SHARE, int(sixteenths)))
+
     def SetTileQubits(self, k: int) -> None:
         """Run fused gate streams as shared-memory tile passes spanning k positions (0 = off,
         register sweeps only); a tuning choice that changes results only by rounding (gates
