@@ -36,6 +36,23 @@ UNIT = "GB/s"
 FALLBACK_HBM_GBS = 6800.0
 
 
+def max_over_ranks(value: float, dist=None, device: str = "cuda") -> float:
+    """The largest value over all ranks (the slowest replica's time); value itself when
+    running alone."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gbs(world: int, bytes_per_rank: int, seconds: float) -> float:
+    """Whole-job throughput: every replica moves bytes_per_rank in `seconds` (the max over
+    ranks)."""
+    return world * bytes_per_rank / seconds / 1e9
+
+
 def layer_bytes(n: int, amp_bytes: int = 16) -> int:
     N = 1 << n
     num_cz = (n // 2) + ((n - 1) // 2)
@@ -315,6 +332,46 @@ def batched_section(count: int = 4096, loop_sample: int = 64) -> dict:
             "max_abs_energy_diff_vs_loop": loop_err}
 
 
+def plain_section(reps: int = 5) -> dict:
+    """The 20-qubit, 780-gate circuit (20 layers of Haar U on every qubit + CNOT bricks) from
+    |0...0>, gate by gate and fused, ComplexDP in native and emulated arithmetic: time per
+    circuit and the error against the amplitudes the reference itself computed
+    (tests/golden/golden.npz, case plain_gate_by_gate_20q); the 16 MiB state stays in L2, so
+    this reports time, not an HBM fraction. The C restatement of the reference's loops runs
+    the same circuit on the host cores for comparison."""
+    import iqs_gb300 as iqs
+    import oracle
+    from circuits import replay
+    z = np.load(REPO / "tests" / "golden" / "golden.npz")
+    name = "plain_gate_by_gate_20q"
+    ops = json.loads(str(z[f"{name}/ops"]))
+    idx, want = z[f"{name}/final_idx"], z[f"{name}/final"]
+    out = {"workload": "20 qubits, 20 layers of (Haar U on every qubit + CNOT bricks), 780 gates, ComplexDP",
+           "gates": len(ops)}
+    for math in ("native", "emulated"):
+        for fusion in (False, True):
+            reg = iqs.QubitRegister(20, "base", 0, math=math)
+            best = float("inf")
+            for _ in range(reps):
+                reg.Initialize("base", 0)
+                if fusion:
+                    reg.TurnOnFusion()
+                reg.synchronize()
+                t0 = time.perf_counter()
+                replay(reg, ops)
+                reg.ApplyFusedGates()
+                reg.synchronize()
+                best = min(best, time.perf_counter() - t0)
+            err = float(np.max(np.abs(reg.GetStateVector()[idx] - want)))
+            out[f"{math}{'_fused' if fusion else ''}"] = {"ms": round(best * 1e3, 2), "max_abs_err_vs_reference": err}
+    o = oracle.OracleRegister(20, "base", 0)
+    t0 = time.perf_counter()
+    replay(o, ops)
+    out["cpu_restatement_ms"] = round((time.perf_counter() - t0) * 1e3, 1)
+    out["cpu_threads"] = oracle.get_threads()
+    return out
+
+
 def gate_bytes(ops, n: int, amp_bytes: int) -> int:
     """Algorithmic bytes of a gate list: 2*N*s per 1-qubit gate, N*s per controlled or
     swap-type gate (src/highperfkernels.cpp:370, :478-479)."""
@@ -556,13 +613,9 @@ def run_ours(args) -> None:
     end.record(stream)
     barrier()
     clk = clocks.stop()
-    ms = start.elapsed_time(end)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(start.elapsed_time(end), dist)
     ms_per_step = ms / args.steps
-    value = world * layer_bytes(n) / (ms_per_step * 1e-3) / 1e9
+    value = job_gbs(world, layer_bytes(n), ms_per_step * 1e-3)
 
     # Dominant kernel. Fused: every launch in the timed region is a full pass over the
     # state (2*N*16 bytes), so the average launch time is the region time / launches.
@@ -590,8 +643,8 @@ def run_ours(args) -> None:
         step(args.warmup + s % args.steps)
         reg.GetStateVector(out=hbuf)                  # HBM -> host (pinned)
     barrier()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e_value = world * layer_bytes(n) / e2e_s / 1e9
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dist)
+    e2e_value = job_gbs(world, layer_bytes(n), e2e_s)
 
     # Same layer with native FP64 arithmetic, for comparison (2 steps).
     other = {}
@@ -618,6 +671,7 @@ def run_ours(args) -> None:
     batched = None
     qft = None
     trotter = None
+    plain = None
     if rank == 0:
         import oracle
         oracle.build(ref=False)
@@ -638,6 +692,7 @@ def run_ours(args) -> None:
             cpu = cpu_layer_gbs(args.cpu_qubits, 1, seed=5, threads=threads)
         qaoa = None if args.no_adjoint else qaoa_section(stream=stream.cuda_stream)
         batched = None if args.no_batched else batched_section()
+        plain = plain_section()
         qft = None if args.no_qft else qft_brick_section()
         trotter = None if args.no_trotter else trotter_section(grad_steps=100 if args.full_trotter else 10)
 
@@ -676,6 +731,8 @@ def run_ours(args) -> None:
             line["adjoint"] = qaoa
         if batched is not None:
             line["batched"] = batched
+        if plain is not None:
+            line["plain_gate_by_gate_20q"] = plain
         if qft is not None:
             line["qft_brick"] = qft
         if trotter is not None:

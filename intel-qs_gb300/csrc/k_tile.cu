@@ -259,6 +259,7 @@ __global__ void k_tile_grad_finish(const double* __restrict__ partials, unsigned
 
 unsigned entries_of(const SweepOp& op) {
   switch (op.kind) {
+    case SW_CZSHIFT: return 0;
     case SW_PHASE: return 1;
     case SW_U2: case SW_SWAPLIKE: case SW_GRAD1: return 4;
     case SW_EXC: case SW_GRADEXC: return 6;

@@ -93,6 +93,24 @@ class SweepBuilder {
 
   void add_phase(uint64_t mask, uint64_t value, double re, double im) {
     if (is_one(re, im)) return;
+    // A CZ (phase -1 where two bits are both set) joins the preceding CZ-run op of the same
+    // bit distance: the product of CZ(a, a + d) over a set A of low bits is
+    // (-1)^popcount(x & (x >> d) & A), and a repeated pair cancels (XOR into A).
+    if (re == -1.0 && im == 0.0 && value == mask && __builtin_popcountll(mask) == 2) {
+      const unsigned a = (unsigned)__builtin_ctzll(mask), b = 63u - (unsigned)__builtin_clzll(mask);
+      const unsigned d = b - a;
+      if (P_.nops && P_.ops[P_.nops - 1].kind == SW_CZSHIFT && P_.ops[P_.nops - 1].j0 == d) {
+        P_.ops[P_.nops - 1].mask ^= uint64_t(1) << a;
+        return;
+      }
+      reserve({}, 1, 0);
+      SweepOp op{};
+      op.kind = SW_CZSHIFT;
+      op.j0 = (uint8_t)d;
+      op.mask = uint64_t(1) << a;
+      P_.ops[P_.nops++] = op;
+      return;
+    }
     reserve({}, 1, 1);
     SweepOp op{};
     op.kind = SW_PHASE;

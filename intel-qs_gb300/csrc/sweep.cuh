@@ -32,6 +32,8 @@ enum SweepKind : uint8_t {
                     // scales |00>, entries 1-4 are the 2x2 on (|lo=1,hi=0>, |lo=0,hi=1>), entry 5
                     // scales |11>; where (idx & mask) == mask
   SW_GRADEXC = 7,   // adjoint sweeps only: Im <w|M|v> for M with the SW_EXC layout
+  SW_CZSHIFT = 8,   // amp *= (-1)^popcount(idx & (idx >> j0) & mask): the product of CZ(a, a + j0)
+                    // over the bits a of mask (exact sign flips)
 };
 
 enum SweepFlags : uint8_t {
@@ -292,6 +294,18 @@ __device__ __forceinline__ void op_phase(const SweepEntry* E, const SweepOp& op,
   }
 }
 
+template <typename A, int K>
+__device__ __forceinline__ void op_czshift(const SweepOp& op, typename A::VT* v, const uint64_t* idx, unsigned& tm) {
+  constexpr int G = 1 << K;
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if (__popcll(idx[s] & (idx[s] >> op.j0) & op.mask) & 1) {
+      vt_neg(v[s]);
+      tm |= 1u << s;
+    }
+  }
+}
+
 // One operation on one group. A runtime active-bit index is dispatched to a compile-time
 // one, so the group stays in registers (no dynamic register indexing).
 template <typename A, int K>
@@ -300,6 +314,9 @@ __device__ __forceinline__ void apply_op(const SweepEntry* E, const SweepOp& op,
   switch (op.kind) {
     case SW_PHASE:
       op_phase<A, K>(E, op, v, idx, tm);
+      break;
+    case SW_CZSHIFT:
+      op_czshift<A, K>(op, v, idx, tm);
       break;
     case SW_U2:
       if constexpr (K >= 1) {

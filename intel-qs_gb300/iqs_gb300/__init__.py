@@ -13,6 +13,7 @@ from .permutation import GateCounter, Permutation
 from .qureg import QubitRegister
 from .adjoint import QaoaMaxCut, qaoa_energy
 from .batched import BatchedAnsatz
+from .trotter import XXZChain
 from .qaoa import (GetExpectationValueFromCostFunction, GetExpectationValueSquaredFromCostFunction,
                    ImplementQaoaLayerBasedOnCostFunction, InitializeVectorAsMaxCutCostFunction)
 
@@ -20,5 +21,5 @@ __all__ = [
     "QubitRegister", "Permutation", "GateCounter", "IqsgError", "LIB_PATH", "lib",
     "InitializeVectorAsMaxCutCostFunction", "ImplementQaoaLayerBasedOnCostFunction",
     "GetExpectationValueFromCostFunction", "GetExpectationValueSquaredFromCostFunction",
-    "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz",
+    "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz", "XXZChain",
 ]
