@@ -346,8 +346,9 @@ def plain_section(reps: int = 5) -> dict:
     name = "plain_gate_by_gate_20q"
     ops = json.loads(str(z[f"{name}/ops"]))
     idx, want = z[f"{name}/final_idx"], z[f"{name}/final"]
+    from circuits import QUERIES
     out = {"workload": "20 qubits, 20 layers of (Haar U on every qubit + CNOT bricks), 780 gates, ComplexDP",
-           "gates": len(ops)}
+           "gates": sum(1 for name, _ in ops if name not in QUERIES)}
     for math in ("native", "emulated"):
         for fusion in (False, True):
             reg = iqs.QubitRegister(20, "base", 0, math=math)
@@ -629,6 +630,16 @@ def run_ours(args) -> None:
         kname = "k_1q_df (1-qubit gate, emulated FP64)" if args.math == "emulated" else "k_1q<double>"
     peak, peak_src = peak_hbm()
     achieved = 2 * (1 << n) * 16 / (k_avg * 1e-3) / 1e9
+    # DRAM bytes per launch: given on the command line, else the ratio ncu measured for the
+    # fused emulated pass on a 27-qubit state (4.234 GB read + written per 4.295 GB pass; the
+    # capture is too large to repeat at 30 qubits), scaled by the amplitudes of this pass.
+    if args.traffic is not None:
+        traffic, traffic_src = args.traffic, "command line"
+    elif args.fusion and args.math == "emulated" and (args.width or (tuned and tuned["width"])) == 2:
+        traffic = round(4.234e9 / 4.295e9 * 2 * (1 << n) * 16)
+        traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_sweep_df<2> at 27 qubits, scaled"
+    else:
+        traffic, traffic_src = None, None
 
     # End to end through the public API with host buffers: upload the state from pinned
     # host memory, apply the layer, download the state, every step.
@@ -703,7 +714,7 @@ def run_ours(args) -> None:
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic (seeded Haar-random gates on a dense state)",
-            "config": {"workload": f"gate layer: Haar U on each of {n} qubits + CZ brick (15 even + 14 odd), ComplexDP",
+            "config": {"workload": f"gate layer: Haar U on each of {n} qubits + CZ brick ({n // 2} even + {(n - 1) // 2} odd), ComplexDP",
                        "qubits": n, "state_bytes": (1 << n) * 16, "bytes_per_step": layer_bytes(n),
                        "math": args.math, "fusion": bool(args.fusion),
                        "sweep_width": args.width or (tuned["width"] if tuned else "default"),
@@ -713,12 +724,12 @@ def run_ours(args) -> None:
                        "autotune_ms": [[r["width"], r["pipeline"], r["native_share"], round(r["ms"], 1)]
                                        for r in tuned["table"]] if tuned else None,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "state (16 GiB) far larger than L2 (129 MB); no flush needed"},
+                       "l2": f"state ({(1 << n) * 16 / 2**30:g} GiB) far larger than L2 (129 MB); no flush needed"},
             "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_src,
                          "bytes_per_launch": 2 * (1 << n) * 16, "avg_launch_ms": round(k_avg, 4),
-                         "traffic": args.traffic},
+                         "traffic": traffic, "traffic_source": traffic_src},
             "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": (1 << n) * 16,
                     "d2h_bytes_per_step": (1 << n) * 16, "steps": e2e_steps,
                     "path": "QubitRegister.SetStateVector (pinned host) + layer via public API + iqsg_download (pinned host)"},
@@ -773,13 +784,37 @@ def main() -> None:
                     help="adjoint gradient over all 100 Strang steps at 32 qubits (about 1.5 min more)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per 1-qubit-gate launch from an ncu capture, if known")
+    ap.add_argument("--only", choices=["plain", "adjoint", "batched", "qft", "trotter"], default=None,
+                    help="run one section alone and print its JSON (a profiling entry point; not the bench line)")
+    ap.add_argument("--section-qubits", type=int, default=0, help="with --only: register size of the section")
+    ap.add_argument("--section-steps", type=int, default=0, help="with --only trotter: Strang steps")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.only:
+        run_section(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
+
+
+def run_section(args) -> None:
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    q, st = args.section_qubits, args.section_steps
+    if args.only == "plain":
+        out = plain_section()
+    elif args.only == "adjoint":
+        out = qaoa_section(n=q or 26)
+    elif args.only == "batched":
+        out = batched_section(count=q or 4096)
+    elif args.only == "qft":
+        out = qft_brick_section(n=q or 30)
+    else:
+        out = trotter_section(n=q or 32, steps=st or 100, n_dp=(q + 1) if q else 33, steps_dp=4,
+                              grad_steps=min(st or 10, 10))
+    print(json.dumps({"section": args.only, **out}), flush=True)
 
 
 if __name__ == "__main__":
