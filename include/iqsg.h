@@ -112,6 +112,13 @@ int iqsg_get_amplitude(iqsg_state* h, uint64_t data_index, double* re_im);
 int iqsg_upload(iqsg_state* h, const void* host, uint64_t offset, uint64_t count);
 int iqsg_download(iqsg_state* h, void* host, uint64_t offset, uint64_t count);
 
+/* The same copies queued on the register's stream without waiting: they run in order with the
+ * register's gates, so a caller can overlap one register's transfers with another register's
+ * work. The host memory must stay valid, and unread (upload) or untouched (download), until
+ * iqsg_synchronize returns; with pinned host memory the call returns at once. */
+int iqsg_upload_async(iqsg_state* h, const void* host, uint64_t offset, uint64_t count);
+int iqsg_download_async(iqsg_state* h, void* host, uint64_t offset, uint64_t count);
+
 /* Device-to-device copy of all amplitudes (same size and precision). */
 int iqsg_copy(iqsg_state* dst, const iqsg_state* src);
 
@@ -342,8 +349,8 @@ int iqsg_batch_destroy(iqsg_batch* b);
  * params, energies and grads are host arrays. */
 int iqsg_batch_run(iqsg_batch* b, const double* params, int with_grad, double* energies, double* grads);
 
-/* Launch shape of the persistent kernel (threads per CTA, CTAs per SM); chosen by the
- * autotuner. Invalidates the recorded graphs. */
+/* Launch shape of the persistent kernel (threads per CTA: 32..512, a multiple of 32; CTAs per
+ * SM: 1..16); chosen by the autotuner. Invalidates the recorded graphs. */
 int iqsg_batch_set_launch(iqsg_batch* b, unsigned threads, unsigned ctas_per_sm);
 int iqsg_batch_info(const iqsg_batch* b, uint64_t* num_params, uint64_t* total_amplitudes);
 

@@ -422,6 +422,26 @@ int iqsg_download(iqsg_state* h, void* host, uint64_t offset, uint64_t count) {
   return sync_and_check(h, "iqsg_download");
 }
 
+int iqsg_upload_async(iqsg_state* h, const void* host, uint64_t offset, uint64_t count) {
+  int st = check_h(h);
+  if (st) return st;
+  if (!host && count) return fail(IQSG_EINVAL, "iqsg_upload_async: null host pointer");
+  if (offset > h->N || count > h->N - offset) return fail(IQSG_EINVAL, "iqsg_upload_async: range out of bounds");
+  const size_t b = amp_bytes(h->prec);
+  return cuda_status(cudaMemcpyAsync((char*)h->amps + offset * b, host, count * b, cudaMemcpyHostToDevice, h->stream),
+                     "iqsg_upload_async");
+}
+
+int iqsg_download_async(iqsg_state* h, void* host, uint64_t offset, uint64_t count) {
+  int st = check_h(h);
+  if (st) return st;
+  if (!host && count) return fail(IQSG_EINVAL, "iqsg_download_async: null host pointer");
+  if (offset > h->N || count > h->N - offset) return fail(IQSG_EINVAL, "iqsg_download_async: range out of bounds");
+  const size_t b = amp_bytes(h->prec);
+  return cuda_status(cudaMemcpyAsync(host, (const char*)h->amps + offset * b, count * b, cudaMemcpyDeviceToHost,
+                                     h->stream), "iqsg_download_async");
+}
+
 int iqsg_copy(iqsg_state* dst, const iqsg_state* src) {
   int st = check_pair(dst, src, "iqsg_copy");
   if (st) return st;

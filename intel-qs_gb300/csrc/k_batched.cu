@@ -5,8 +5,9 @@
 // to every qubit and then CZ(q, q+1) for q = 0..n-2. Its observable is a sum of Pauli strings
 // c_k P_k. The persistent grid pulls instances (largest first) from an atomic work counter;
 // one CTA owns an instance at a time and keeps its two state vectors (psi and lambda = O psi)
-// in a per-instance slice of device memory, applying gate after gate with CTA barriers in
-// between. Gradients follow the adjoint method: walking the circuit backwards,
+// in a per-instance slice of device memory; each pass over the instance applies the rotations
+// of three qubits to groups of 8 amplitudes held in registers (the CZ ladder rides on the
+// pass holding the last qubit), with a CTA barrier between passes. Gradients follow the adjoint method: walking the circuit backwards,
 // dE/dtheta = Im <lambda|Y_q|psi> and dE/dphi = Im <lambda|Z_q|psi> at the point after the
 // gate, then the gate is undone on both vectors. All sums are FP64 in a fixed order per CTA.
 #include <algorithm>
@@ -121,8 +122,150 @@ __device__ __forceinline__ void apply2(const Mat<R>& M, CXb<R>& a, CXb<R>& b) {
   b = o1;
 }
 
+// Forward: RZ then RY on qubits q0 .. q0+W-1 of one layer in a single pass over groups of 2^W
+// amplitudes (the W qubits' index bits), in qubit order; the layer's CZ ladder rides on the
+// pass that holds the last qubit.
+template <typename R, int W>
+__device__ __forceinline__ void fwd_chunk(typename V2<R>::type* __restrict__ psi, uint64_t N, unsigned q0,
+                                          const double* prm_l, bool last, uint64_t ladder) {
+  using V = typename V2<R>::type;
+  constexpr int G = 1 << W;
+  Mat<R> M[W];
+#pragma unroll
+  for (int k = 0; k < W; ++k) M[k] = ry_rz<R>(prm_l[2 * (q0 + k) + 1], prm_l[2 * (q0 + k)]);
+  const uint64_t groups = N >> W, lowmask = (uint64_t(1) << q0) - 1;
+  for (uint64_t p = threadIdx.x; p < groups; p += blockDim.x) {
+    const uint64_t base = (p & lowmask) | ((p >> q0) << (q0 + W));
+    CXb<R> a[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      const V v = psi[base | ((uint64_t)j << q0)];
+      a[j].re = v.x;
+      a[j].im = v.y;
+    }
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+#pragma unroll
+      for (int j = 0; j < G; ++j)
+        if (!(j & (1 << k))) apply2(M[k], a[j], a[j | (1 << k)]);
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      const uint64_t i = base | ((uint64_t)j << q0);
+      if (last && (__popcll(i & (i >> 1) & ladder) & 1)) {
+        a[j].re = -a[j].re;
+        a[j].im = -a[j].im;
+      }
+      V o;
+      o.x = a[j].re;
+      o.y = a[j].im;
+      psi[i] = o;
+    }
+  }
+}
+
+// Backward over the same W qubits (last first): undo the CZ ladder if this pass holds the last
+// qubit, then per qubit the RY gradient Im <lambda|Y|psi>, undo RY, the RZ gradient
+// Im <lambda|Z|psi>, undo RZ, on psi and lambda. Gradient terms are summed in R over
+// kChunk groups and then in FP64 per thread; the block sums land in grd.
+template <typename R, int W>
+__device__ __forceinline__ void bwd_chunk(typename V2<R>::type* __restrict__ psi, typename V2<R>::type* __restrict__ lam,
+                                          uint64_t N, unsigned q0, const double* prm_l, bool last, uint64_t ladder,
+                                          double* grd_l, double* s_red) {
+  using V = typename V2<R>::type;
+  constexpr int G = 1 << W;
+  R c[W], s[W], zc[W], zs[W];
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    double st, ct, sp, cp;
+    sincos(0.5 * prm_l[2 * (q0 + k) + 1], &st, &ct);
+    sincos(0.5 * prm_l[2 * (q0 + k)], &sp, &cp);
+    c[k] = (R)ct;
+    s[k] = (R)st;
+    zc[k] = (R)cp;
+    zs[k] = (R)sp;
+  }
+  double gy[W], gz[W];
+  R cy[W], cz[W];
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    gy[k] = gz[k] = 0.0;
+    cy[k] = cz[k] = 0;
+  }
+  unsigned cnt = 0;
+  const uint64_t groups = N >> W, lowmask = (uint64_t(1) << q0) - 1;
+  for (uint64_t p = threadIdx.x; p < groups; p += blockDim.x) {
+    const uint64_t base = (p & lowmask) | ((p >> q0) << (q0 + W));
+    V ps[G], ls[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      const uint64_t i = base | ((uint64_t)j << q0);
+      ps[j] = psi[i];
+      ls[j] = lam[i];
+      if (last && (__popcll(i & (i >> 1) & ladder) & 1)) {  // the CZ ladder is its own inverse
+        ps[j].x = -ps[j].x; ps[j].y = -ps[j].y;
+        ls[j].x = -ls[j].x; ls[j].y = -ls[j].y;
+      }
+    }
+#pragma unroll
+    for (int k = W - 1; k >= 0; --k) {
+#pragma unroll
+      for (int j = 0; j < G; ++j) {
+        if (j & (1 << k)) continue;
+        const int j1 = j | (1 << k);
+        const V p0 = ps[j], p1 = ps[j1], l0 = ls[j], l1 = ls[j1];
+        cy[k] += (l1.x * p0.x + l1.y * p0.y) - (l0.x * p1.x + l0.y * p1.y);
+        V a0, a1, b0, b1;
+        a0.x = c[k] * p0.x + s[k] * p1.x; a0.y = c[k] * p0.y + s[k] * p1.y;
+        a1.x = c[k] * p1.x - s[k] * p0.x; a1.y = c[k] * p1.y - s[k] * p0.y;
+        b0.x = c[k] * l0.x + s[k] * l1.x; b0.y = c[k] * l0.y + s[k] * l1.y;
+        b1.x = c[k] * l1.x - s[k] * l0.x; b1.y = c[k] * l1.y - s[k] * l0.y;
+        cz[k] += (b0.x * a0.y - b0.y * a0.x) - (b1.x * a1.y - b1.y * a1.x);
+        V o;
+        o.x = zc[k] * a0.x - zs[k] * a0.y; o.y = zc[k] * a0.y + zs[k] * a0.x; ps[j] = o;
+        o.x = zc[k] * a1.x + zs[k] * a1.y; o.y = zc[k] * a1.y - zs[k] * a1.x; ps[j1] = o;
+        o.x = zc[k] * b0.x - zs[k] * b0.y; o.y = zc[k] * b0.y + zs[k] * b0.x; ls[j] = o;
+        o.x = zc[k] * b1.x + zs[k] * b1.y; o.y = zc[k] * b1.y - zs[k] * b1.x; ls[j1] = o;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      const uint64_t i = base | ((uint64_t)j << q0);
+      psi[i] = ps[j];
+      lam[i] = ls[j];
+    }
+    if (++cnt == kChunk) {
+      cnt = 0;
+#pragma unroll
+      for (int k = 0; k < W; ++k) {
+        gy[k] += (double)cy[k];
+        gz[k] += (double)cz[k];
+        cy[k] = cz[k] = 0;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    double y = gy[k] + (double)cy[k], z = gz[k] + (double)cz[k];
+    block_sum2(y, z, s_red);
+    if (threadIdx.x == 0) {
+      grd_l[2 * (q0 + k) + 1] = y;
+      grd_l[2 * (q0 + k)] = z;
+    }
+    __syncthreads();
+  }
+}
+
+// Qubits per pass: 3 in FP32 (8-amplitude groups, 127 registers), 2 in FP64 (the 3-qubit
+// FP64 variant needs 168 registers).
 template <typename R>
-__global__ void k_batched(unsigned count, const unsigned* __restrict__ order, const uint32_t* __restrict__ meta,
+constexpr unsigned qubits_per_pass() {
+  return sizeof(R) == 4 ? 3u : 2u;
+}
+
+constexpr unsigned kBatchMaxThreads = 512;
+
+template <typename R>
+__global__ void __launch_bounds__(kBatchMaxThreads) k_batched(unsigned count, const unsigned* __restrict__ order, const uint32_t* __restrict__ meta,
                           const uint64_t* __restrict__ state_off, const uint64_t* __restrict__ param_off,
                           const iqsg_pauli_term* __restrict__ terms, typename V2<R>::type* __restrict__ psi_all,
                           typename V2<R>::type* __restrict__ lam_all, const double* __restrict__ params,
@@ -139,7 +282,7 @@ __global__ void k_batched(unsigned count, const unsigned* __restrict__ order, co
     if (item >= count) return;
     const unsigned inst = order[item];
     const unsigned n = meta[4 * inst], L = meta[4 * inst + 1], nt = meta[4 * inst + 2], t0 = meta[4 * inst + 3];
-    const uint64_t N = uint64_t(1) << n, half = N >> 1;
+    const uint64_t N = uint64_t(1) << n;
     V* psi = psi_all + state_off[inst];
     V* lam = lam_all + state_off[inst];
     const double* prm = params + param_off[inst];
@@ -156,23 +299,18 @@ __global__ void k_batched(unsigned count, const unsigned* __restrict__ order, co
     }
     __syncthreads();
     for (unsigned l = 0; l < L; ++l) {
-      for (unsigned q = 0; q < n; ++q) {
-        const Mat<R> M = ry_rz<R>(prm[2 * (l * n + q) + 1], prm[2 * (l * n + q)]);
-        const uint64_t d = uint64_t(1) << q;
-        const bool last = q + 1 == n;  // the CZ ladder rides on the last rotation pass
-        for (uint64_t p = tid; p < half; p += nth) {
-          const uint64_t i0 = insert_zero(p, q), i1 = i0 | d;
-          const V va = psi[i0], vb = psi[i1];
-          CXb<R> a{va.x, va.y}, b{vb.x, vb.y};
-          apply2(M, a, b);
-          if (last) {
-            if (__popcll(i0 & (i0 >> 1) & ladder) & 1) { a.re = -a.re; a.im = -a.im; }
-            if (__popcll(i1 & (i1 >> 1) & ladder) & 1) { b.re = -b.re; b.im = -b.im; }
-          }
-          V oa, ob;
-          oa.x = a.re; oa.y = a.im; ob.x = b.re; ob.y = b.im;
-          psi[i0] = oa;
-          psi[i1] = ob;
+      const double* prm_l = prm + 2 * (uint64_t)l * n;
+      constexpr unsigned QP = qubits_per_pass<R>();
+      for (unsigned q0 = 0; q0 < n; q0 += QP) {
+        const unsigned w = n - q0 < QP ? n - q0 : QP;
+        const bool last = q0 + w == n;
+        if constexpr (QP == 3) {
+          if (w == 3) fwd_chunk<R, 3>(psi, N, q0, prm_l, last, ladder);
+          else if (w == 2) fwd_chunk<R, 2>(psi, N, q0, prm_l, last, ladder);
+          else fwd_chunk<R, 1>(psi, N, q0, prm_l, last, ladder);
+        } else {
+          if (w == 2) fwd_chunk<R, 2>(psi, N, q0, prm_l, last, ladder);
+          else fwd_chunk<R, 1>(psi, N, q0, prm_l, last, ladder);
         }
         __syncthreads();
       }
@@ -210,58 +348,24 @@ __global__ void k_batched(unsigned count, const unsigned* __restrict__ order, co
     if (tid == 0) energy[inst] = etot;
     __syncthreads();
     if (!with_grad) continue;
-    // ---- backward: one pass per qubit (undo the CZ ladder on the first, then RY and RZ) ----
+    // ---- backward: the same passes, layers and qubits in reverse ----
     for (int l = (int)L - 1; l >= 0; --l) {
-      for (int q = (int)n - 1; q >= 0; --q) {
-        const double theta = prm[2 * (l * n + q) + 1], phi = prm[2 * (l * n + q)];
-        const uint64_t d = uint64_t(1) << q;
-        const bool first = q == (int)n - 1;
-        double st, ct, sp, cp;
-        sincos(0.5 * theta, &st, &ct);
-        sincos(0.5 * phi, &sp, &cp);
-        const R c = (R)ct, s = (R)st, zc = (R)cp, zs = (R)sp;
-        // Products and short partial sums in R; every kChunk pairs the partials move into FP64
-        // (FP64 arithmetic per pair would bound the pass on the FP64 pipe).
-        double gy = 0.0, gz = 0.0;
-        R cy = 0, cz = 0;
-        unsigned cnt = 0;
-        for (uint64_t pidx = tid; pidx < half; pidx += nth) {
-          const uint64_t i0 = insert_zero(pidx, q), i1 = i0 | d;
-          V p0 = psi[i0], p1 = psi[i1], l0 = lam[i0], l1 = lam[i1];
-          if (first) {  // the CZ ladder is its own inverse
-            if (__popcll(i0 & (i0 >> 1) & ladder) & 1) { p0.x = -p0.x; p0.y = -p0.y; l0.x = -l0.x; l0.y = -l0.y; }
-            if (__popcll(i1 & (i1 >> 1) & ladder) & 1) { p1.x = -p1.x; p1.y = -p1.y; l1.x = -l1.x; l1.y = -l1.y; }
-          }
-          // RY(theta): Im <lambda|Y_q|psi> = -Re(conj(l0) p1) + Re(conj(l1) p0), then undo RY.
-          cy += (l1.x * p0.x + l1.y * p0.y) - (l0.x * p1.x + l0.y * p1.y);
-          V a0, a1, b0, b1;
-          a0.x = c * p0.x + s * p1.x; a0.y = c * p0.y + s * p1.y;
-          a1.x = c * p1.x - s * p0.x; a1.y = c * p1.y - s * p0.y;
-          b0.x = c * l0.x + s * l1.x; b0.y = c * l0.y + s * l1.y;
-          b1.x = c * l1.x - s * l0.x; b1.y = c * l1.y - s * l0.y;
-          // RZ(phi): Im <lambda|Z_q|psi> (bit 0: +, bit 1: -), then undo RZ
-          // (multiply by e^{+i phi/2} on bit 0, e^{-i phi/2} on bit 1).
-          cz += (b0.x * a0.y - b0.y * a0.x) - (b1.x * a1.y - b1.y * a1.x);
-          if (++cnt == kChunk) {
-            gy += (double)cy;
-            gz += (double)cz;
-            cy = cz = 0;
-            cnt = 0;
-          }
-          V o;
-          o.x = zc * a0.x - zs * a0.y; o.y = zc * a0.y + zs * a0.x; psi[i0] = o;
-          o.x = zc * a1.x + zs * a1.y; o.y = zc * a1.y - zs * a1.x; psi[i1] = o;
-          o.x = zc * b0.x - zs * b0.y; o.y = zc * b0.y + zs * b0.x; lam[i0] = o;
-          o.x = zc * b1.x + zs * b1.y; o.y = zc * b1.y - zs * b1.x; lam[i1] = o;
+      const double* prm_l = prm + 2 * (uint64_t)l * n;
+      double* grd_l = grd + 2 * (uint64_t)l * n;
+      constexpr unsigned QP = qubits_per_pass<R>();
+      const unsigned nchunks = (n + QP - 1) / QP;
+      for (int c = (int)nchunks - 1; c >= 0; --c) {
+        const unsigned q0 = (unsigned)c * QP;
+        const unsigned w = n - q0 < QP ? n - q0 : QP;
+        const bool last = q0 + w == n;
+        if constexpr (QP == 3) {
+          if (w == 3) bwd_chunk<R, 3>(psi, lam, N, q0, prm_l, last, ladder, grd_l, s_red);
+          else if (w == 2) bwd_chunk<R, 2>(psi, lam, N, q0, prm_l, last, ladder, grd_l, s_red);
+          else bwd_chunk<R, 1>(psi, lam, N, q0, prm_l, last, ladder, grd_l, s_red);
+        } else {
+          if (w == 2) bwd_chunk<R, 2>(psi, lam, N, q0, prm_l, last, ladder, grd_l, s_red);
+          else bwd_chunk<R, 1>(psi, lam, N, q0, prm_l, last, ladder, grd_l, s_red);
         }
-        gy += (double)cy;
-        gz += (double)cz;
-        block_sum2(gy, gz, s_red);
-        if (tid == 0) {
-          grd[2 * (l * n + q) + 1] = gy;
-          grd[2 * (l * n + q)] = gz;
-        }
-        __syncthreads();
       }
     }
   }
@@ -415,7 +519,8 @@ extern "C" int iqsg_batch_destroy(iqsg_batch* b) {
 
 extern "C" int iqsg_batch_set_launch(iqsg_batch* b, unsigned threads, unsigned ctas_per_sm) {
   if (!b) return fail(IQSG_EINVAL, "null batch handle");
-  if (threads < 32 || threads > 1024 || threads % 32) return fail(IQSG_EINVAL, "iqsg_batch_set_launch: threads %u", threads);
+  if (threads < 32 || threads > kBatchMaxThreads || threads % 32)
+    return fail(IQSG_EINVAL, "iqsg_batch_set_launch: threads %u (32..%u, a multiple of 32)", threads, kBatchMaxThreads);
   if (ctas_per_sm < 1 || ctas_per_sm > 16) return fail(IQSG_EINVAL, "iqsg_batch_set_launch: ctas_per_sm %u", ctas_per_sm);
   b->threads = threads;
   b->ctas_per_sm = ctas_per_sm;

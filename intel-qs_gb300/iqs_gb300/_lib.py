@@ -62,6 +62,8 @@ SIGNATURES = {
     "iqsg_get_amplitude": [_P, _U64, _DP],
     "iqsg_upload": [_P, _P, _U64, _U64],
     "iqsg_download": [_P, _P, _U64, _U64],
+    "iqsg_upload_async": [_P, _P, _U64, _U64],
+    "iqsg_download_async": [_P, _P, _U64, _U64],
     "iqsg_copy": [_P, _P],
     "iqsg_apply_1q": [_P, _U, _DP],
     "iqsg_apply_controlled_1q": [_P, _U, _U, _DP],

@@ -88,7 +88,7 @@ class BatchedAnsatz:
         return (e, g) if with_grad else e
 
     def autotune(self, params, with_grad: bool = True,
-                 shapes=((128, 4), (256, 2), (256, 4), (512, 1), (512, 2), (1024, 1), (1024, 2)), trials: int = 2):
+                 shapes=((128, 4), (128, 8), (256, 2), (256, 4), (512, 1), (512, 2)), trials: int = 2):
         """Time every (threads per CTA, CTAs per SM) and keep the fastest; returns the table."""
         table = []
         for th, cps in shapes:

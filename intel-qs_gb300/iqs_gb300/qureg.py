@@ -206,6 +206,24 @@ class QubitRegister:
             raise ValueError(f"expected {self.GlobalSize()} amplitudes, got shape {a.shape}")
         check(lib.iqsg_upload(self._h, a.ctypes.data_as(C.c_void_p), 0, a.size))
 
+    def SetStateVectorAsync(self, amps: np.ndarray) -> None:
+        """Queue the upload of all amplitudes from a contiguous host array of this register's
+        dtype (pinned memory makes it asynchronous); it runs in order with the register's
+        gates. Keep the array alive and unchanged until synchronize()."""
+        self._flush()
+        if amps.dtype != self.dtype or amps.shape != (self.GlobalSize(),) or not amps.flags.c_contiguous:
+            raise ValueError("SetStateVectorAsync: amps must be a contiguous array of this register's size and dtype")
+        check(lib.iqsg_upload_async(self._h, amps.ctypes.data_as(C.c_void_p), 0, amps.size))
+
+    def GetStateVectorAsync(self, out: np.ndarray) -> np.ndarray:
+        """Queue the download of all amplitudes into `out` (contiguous, this register's dtype);
+        the data is there after synchronize()."""
+        self._flush()
+        if out.dtype != self.dtype or out.shape != (self.GlobalSize(),) or not out.flags.c_contiguous:
+            raise ValueError("GetStateVectorAsync: out must be a contiguous array of this register's size and dtype")
+        check(lib.iqsg_download_async(self._h, out.ctypes.data_as(C.c_void_p), 0, out.size))
+        return out
+
     def __array__(self, dtype=None, copy=None):
         a = self.GetStateVector()
         return a if dtype is None else a.astype(dtype)
