@@ -284,6 +284,26 @@ int iqsg_cost_expectation(iqsg_state* psi, const iqsg_state* diag, int power, do
  * InitializeVectorAsMaxCutCostFunction: src/qaoa_features.cpp:73-143. */
 int iqsg_maxcut_cost(iqsg_state* diag, const int* adj, const unsigned* map, int* max_cut);
 
+/* Weighted MaxCut cost vector: Re diag[x] = sum over edges (u, v) of adj[u*n + v] where the
+ * program bits u and v of x differ (adj: n*n doubles, symmetric, zero diagonal), computed in
+ * FP64 and stored in the register's precision; *max_cut (may be NULL) receives the largest
+ * value. Replaces InitializeVectorAsWeightedMaxCutCostFunction: src/qaoa_features.cpp:153-239. */
+int iqsg_weighted_maxcut_cost(iqsg_state* diag, const double* adj, const unsigned* map, double* max_cut);
+
+/* Histogram of |psi_x|^2 over the cost values Re diag[x], FP64 sums in a fixed order:
+ *   IQSG_HIST_INTEGER: bin (int)cost, num_bins = max_value + 1
+ *                      (GetHistogramFromCostFunction, src/qaoa_features.cpp:335-400);
+ *   IQSG_HIST_ROUNDED: bin floor(cost + 1e-7), num_bins = floor(max_value) + 1
+ *                      (...WithWeightsRounded, :402-469);
+ *   IQSG_HIST_BINNED:  bin floor(cost / bin_width + 1e-7), num_bins = ceil(max_value / bin_width) + 1
+ *                      (...WithWeightsBinned, :471-538).
+ * num_bins must equal that count (at most 4096). A cost outside [0, max_value] (or, for the
+ * weighted modes, outside [-1e-7, max_value + 1e-7]) fails with IQSG_EINVAL, where the
+ * reference asserts. Waits for the result. */
+typedef enum { IQSG_HIST_INTEGER = 0, IQSG_HIST_ROUNDED = 1, IQSG_HIST_BINNED = 2 } iqsg_hist_mode;
+int iqsg_cost_histogram(iqsg_state* psi, const iqsg_state* diag, int mode, double max_value, double bin_width,
+                        double* hist, unsigned num_bins);
+
 /* ---- QAOA MaxCut circuits and adjoint gradients ---------------------------------------- */
 
 /* One QAOA layer: amp *= exp(-i gamma H_C) with H_C = 1/2 sum_e w_e Z_u Z_v, then

@@ -832,4 +832,97 @@ int iqsg_maxcut_cost(iqsg_state* diag, const int* adj, const unsigned* map, int*
   return IQSG_OK;
 }
 
+int iqsg_weighted_maxcut_cost(iqsg_state* diag, const double* adj, const unsigned* map, double* max_cut) {
+  int st = check_h(diag);
+  if (st) return st;
+  if (!adj) return fail(IQSG_EINVAL, "iqsg_weighted_maxcut_cost: null adjacency");
+  const unsigned n = diag->n;
+  std::vector<unsigned> pmap(n);
+  std::vector<unsigned char> seen(n, 0);
+  for (unsigned q = 0; q < n; ++q) {
+    pmap[q] = map ? map[q] : q;
+    if (pmap[q] >= n || seen[pmap[q]]) return fail(IQSG_EINVAL, "iqsg_weighted_maxcut_cost: map is not a permutation");
+    seen[pmap[q]] = 1;
+  }
+  std::vector<double> edges;
+  for (unsigned v = 0; v < n; ++v) {
+    if (adj[v * n + v] != 0) return fail(IQSG_EINVAL, "iqsg_weighted_maxcut_cost: adjacency diagonal must be zero");
+    for (unsigned u = v + 1; u < n; ++u) {
+      if (adj[v * n + u] != adj[u * n + v])
+        return fail(IQSG_EINVAL, "iqsg_weighted_maxcut_cost: adjacency must be symmetric");
+      if (adj[v * n + u] != 0) {
+        edges.push_back((double)pmap[v]);
+        edges.push_back((double)pmap[u]);
+        edges.push_back(adj[v * n + u]);
+      }
+    }
+  }
+  const unsigned ne = (unsigned)(edges.size() / 3);
+  if (edges.size() > (size_t)2 * kMaxPartials) return fail(IQSG_EINVAL, "iqsg_weighted_maxcut_cost: too many edges");
+  if (ne) {
+    st = cuda_status(cudaMemcpyAsync(diag->scratch, edges.data(), edges.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                     diag->stream), "iqsg_weighted_maxcut_cost: edges");
+    if (st) return st;
+    st = cuda_status(cudaStreamSynchronize(diag->stream), "iqsg_weighted_maxcut_cost");  // edges outlive the copy
+    if (st) return st;
+  }
+  dispatch(diag, [&](auto r) {
+    using R = decltype(r);
+    launch_weighted_cost<R>(diag, diag->scratch, ne);
+  });
+  if ((st = after_launch("iqsg_weighted_maxcut_cost"))) return st;
+  if (!max_cut) return IQSG_OK;
+  dispatch(diag, [&](auto r) {
+    using R = decltype(r);
+    reduce_max_real<R>(diag);
+  });
+  return fetch_results(diag, 1, max_cut, "iqsg_weighted_maxcut_cost");
+}
+
+int iqsg_cost_histogram(iqsg_state* psi, const iqsg_state* diag, int mode, double max_value, double bin_width,
+                        double* hist, unsigned num_bins) {
+  int st = check_pair(psi, diag, "iqsg_cost_histogram");
+  if (st) return st;
+  if (!hist) return fail(IQSG_EINVAL, "iqsg_cost_histogram: null output");
+  if (!(max_value > 0)) return fail(IQSG_EINVAL, "iqsg_cost_histogram: max_value must be positive");
+  long long want;
+  if (mode == IQSG_HIST_INTEGER) {
+    if (max_value != std::floor(max_value)) return fail(IQSG_EINVAL, "iqsg_cost_histogram: max_value must be an integer");
+    want = (long long)max_value + 1;
+  } else if (mode == IQSG_HIST_ROUNDED) {
+    want = (long long)std::floor(max_value) + 1;
+  } else if (mode == IQSG_HIST_BINNED) {
+    if (!(bin_width > 0)) return fail(IQSG_EINVAL, "iqsg_cost_histogram: bin_width must be positive");
+    want = (long long)std::ceil(max_value / bin_width) + 1;
+  } else {
+    return fail(IQSG_EINVAL, "iqsg_cost_histogram: unknown mode %d", mode);
+  }
+  if (want > (long long)kTableDoubles) return fail(IQSG_EINVAL, "iqsg_cost_histogram: more than %d bins", kTableDoubles);
+  if ((long long)num_bins != want)
+    return fail(IQSG_EINVAL, "iqsg_cost_histogram: num_bins %u, this histogram has %lld", num_bins, want);
+  if (diag->stream != psi->stream && (st = cuda_status(cudaStreamSynchronize(diag->stream), "iqsg_cost_histogram")))
+    return st;
+  double* out_dev = psi->scratch + kTableSlot;
+  auto* bad = reinterpret_cast<unsigned long long*>(psi->scratch + kResultSlot + 7);
+  if ((st = cuda_status(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), psi->stream), "iqsg_cost_histogram")))
+    return st;
+  dispatch(psi, [&](auto r) {
+    using R = decltype(r);
+    launch_cost_hist<R>(psi, diag->amps, mode, max_value, bin_width, (int)num_bins, out_dev, bad);
+  });
+  if ((st = after_launch("iqsg_cost_histogram"))) return st;
+  std::vector<double> h(num_bins);
+  unsigned long long nbad = 0;
+  if ((st = cuda_status(cudaMemcpyAsync(h.data(), out_dev, sizeof(double) * num_bins, cudaMemcpyDeviceToHost,
+                                        psi->stream), "iqsg_cost_histogram")))
+    return st;
+  if ((st = cuda_status(cudaMemcpyAsync(&nbad, bad, sizeof nbad, cudaMemcpyDeviceToHost, psi->stream),
+                        "iqsg_cost_histogram")))
+    return st;
+  if ((st = sync_and_check(psi, "iqsg_cost_histogram"))) return st;
+  if (nbad) return fail(IQSG_EINVAL, "iqsg_cost_histogram: %llu cost values outside the histogram range", nbad);
+  for (unsigned b = 0; b < num_bins; ++b) hist[b] = h[b];
+  return IQSG_OK;
+}
+
 }  // extern "C"

@@ -137,6 +137,12 @@ template <typename R> void reduce_max_abs_diff(iqsg_state* h, const void* x, C1<
 template <typename R> void reduce_l2_diff(iqsg_state* h, const void* x);
 template <typename R> void reduce_cost_expectation(iqsg_state* h, const void* diag, int power);
 template <typename R> void reduce_max_real(iqsg_state* h);
+// k_costfn.cu: weighted MaxCut cost vector (edge table of (u, v, w) doubles on the device) and
+// cost histograms (out_dev: nbins device doubles; *bad counts values outside the histogram).
+template <typename R> void launch_weighted_cost(iqsg_state* h, const double* edges, unsigned num_edges);
+template <typename R>
+void launch_cost_hist(iqsg_state* psi, const void* diag, int mode, double max_value, double bin_width, int nbins,
+                      double* out_dev, unsigned long long* bad);
 
 // ---- emulated-FP64 gate kernels (k_emul.cu) ----
 void launch_1q_emulated(iqsg_state* h, unsigned pos, const M2<double>& m);

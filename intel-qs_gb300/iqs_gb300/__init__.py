@@ -15,11 +15,15 @@ from .adjoint import QaoaMaxCut, qaoa_energy
 from .batched import BatchedAnsatz
 from .trotter import XXZChain
 from .qaoa import (GetExpectationValueFromCostFunction, GetExpectationValueSquaredFromCostFunction,
-                   ImplementQaoaLayerBasedOnCostFunction, InitializeVectorAsMaxCutCostFunction)
+                   GetHistogramFromCostFunction, GetHistogramFromCostFunctionWithWeightsBinned,
+                   GetHistogramFromCostFunctionWithWeightsRounded, ImplementQaoaLayerBasedOnCostFunction,
+                   InitializeVectorAsMaxCutCostFunction, InitializeVectorAsWeightedMaxCutCostFunction)
 
 __all__ = [
     "QubitRegister", "Permutation", "GateCounter", "IqsgError", "LIB_PATH", "lib",
     "InitializeVectorAsMaxCutCostFunction", "ImplementQaoaLayerBasedOnCostFunction",
     "GetExpectationValueFromCostFunction", "GetExpectationValueSquaredFromCostFunction",
+    "InitializeVectorAsWeightedMaxCutCostFunction", "GetHistogramFromCostFunction",
+    "GetHistogramFromCostFunctionWithWeightsRounded", "GetHistogramFromCostFunctionWithWeightsBinned",
     "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz", "XXZChain",
 ]

@@ -26,6 +26,7 @@ _UP = C.POINTER(C.c_uint)
 _IP = C.POINTER(C.c_int)
 
 OP_1Q, OP_CTRL, OP_2Q, OP_SWAPLIKE, OP_DIAG2, OP_PHASE, OP_GRAD1, OP_GRAD2 = range(8)
+HIST_INTEGER, HIST_ROUNDED, HIST_BINNED = 0, 1, 2
 
 
 class Op(C.Structure):
@@ -84,6 +85,8 @@ SIGNATURES = {
     "iqsg_l2_diff": [_P, _P, _DP],
     "iqsg_cost_expectation": [_P, _P, C.c_int, _DP],
     "iqsg_maxcut_cost": [_P, _IP, _UP, _IP],
+    "iqsg_weighted_maxcut_cost": [_P, _DP, _UP, _DP],
+    "iqsg_cost_histogram": [_P, _P, C.c_int, _D, _D, _DP, _U],
     "iqsg_apply_ops": [_P, C.POINTER(Op), _U, _UP],
     "iqsg_adjoint_ops": [_P, _P, C.POINTER(Op), _U, _DP, _U, _UP],
     "iqsg_set_sweep_width": [_P, _U],

@@ -399,6 +399,38 @@ def oracle_qaoa_expectation(psi: OracleRegister, diag: OracleRegister, power: in
 _rlib = None
 
 
+def oracle_weighted_maxcut_cost(diag: OracleRegister, adjacency) -> float:
+    """InitializeVectorAsWeightedMaxCutCostFunction through the C restatement."""
+    adj = np.ascontiguousarray(np.asarray(adjacency, dtype=np.float64).reshape(-1))
+    mp = np.asarray(diag.perm.map, dtype=np.uint32)
+    return float(diag._f("qaoa_weighted_cost")(diag._p(), diag.n, adj.ctypes.data_as(_DP), mp.ctypes.data_as(_UP)))
+
+
+def oracle_cost_histogram(psi: OracleRegister, diag: OracleRegister, mode: int, max_value: float,
+                          bin_width: float = 1.0) -> np.ndarray:
+    """The three histogram functions of src/qaoa_features.cpp:335-538 restated with numpy:
+    mode 0 bins (int)cost over 0..max_value; mode 1 floor(cost + 1e-7) over
+    0..floor(max_value); mode 2 floor(cost / bin_width + 1e-7) over 0..ceil(max_value /
+    bin_width). Sums of |psi|^2 in FP64. Raises where the reference asserts."""
+    cost = diag.GetStateVector().real.astype(np.float64)
+    p = np.abs(psi.GetStateVector().astype(np.complex128)) ** 2
+    if mode == 0:
+        b = np.trunc(cost).astype(np.int64)
+        nb = int(max_value) + 1
+        ok = (b >= 0) & (b <= max_value)
+    else:
+        ok = (cost >= -1e-7) & (cost <= max_value + 1e-7)
+        if mode == 1:
+            b = np.floor(cost + 1e-7).astype(np.int64)
+            nb = int(np.floor(max_value)) + 1
+        else:
+            b = np.floor(cost / bin_width + 1e-7).astype(np.int64)
+            nb = int(np.ceil(max_value / bin_width)) + 1
+    if not np.all(ok) or np.any(b >= nb):
+        raise ValueError("cost value outside the histogram range")
+    return np.bincount(b, weights=p, minlength=nb)[:nb]
+
+
 def ref_available() -> bool:
     return REF_LIB.exists()
 
@@ -427,6 +459,8 @@ def rlib() -> C.CDLL:
             "ref_fusion_on": ([_P, _U], None), "ref_fusion_off": ([_P], None),
             "ref_qaoa_maxcut_cost": ([_P, _IP, _U], C.c_int), "ref_qaoa_layer": ([_P, _P, _D], None),
             "ref_qaoa_expectation": ([_P, _P], _D), "ref_qaoa_expectation_sq": ([_P, _P], _D),
+            "ref_qaoa_weighted_cost": ([_P, _DP, _U], _D),
+            "ref_qaoa_histogram": ([_P, _P, C.c_int, _D, _D, _DP, C.c_int], C.c_int),
         }
         for name, (args, res) in sigs.items():
             fn = getattr(L, name)

@@ -170,6 +170,20 @@ double ref_qaoa_expectation(RefReg* psi, RefReg* diag) {
   DISPATCH(psi, r = iqs::qaoa::GetExpectationValueFromCostFunction(*q, *R<T>(diag)));
   return r;
 }
+// mode 0: GetHistogramFromCostFunction, 1: ...WithWeightsRounded, 2: ...WithWeightsBinned.
+// Writes at most cap bins; returns the histogram's length.
+int ref_qaoa_histogram(RefReg* psi, RefReg* diag, int mode, double max_value, double bin_width, double* out, int cap) {
+  int len = 0;
+  DISPATCH(psi, {
+    std::vector<typename QubitRegister<T>::BaseType> h;
+    if (mode == 0) h = iqs::qaoa::GetHistogramFromCostFunction(*q, *R<T>(diag), (int)max_value);
+    else if (mode == 1) h = iqs::qaoa::GetHistogramFromCostFunctionWithWeightsRounded(*q, *R<T>(diag), max_value);
+    else h = iqs::qaoa::GetHistogramFromCostFunctionWithWeightsBinned(*q, *R<T>(diag), max_value, bin_width);
+    len = (int)h.size();
+    for (int i = 0; i < len && i < cap; ++i) out[i] = (double)h[i];
+  });
+  return len;
+}
 double ref_qaoa_expectation_sq(RefReg* psi, RefReg* diag) {
   double r = 0;
   DISPATCH(psi, r = iqs::qaoa::GetExpectationValueSquaredFromCostFunction(*q, *R<T>(diag)));

@@ -6,7 +6,7 @@ import pytest
 
 import oracle
 from circuits import random_circuit, random_state, replay
-from conftest import case_meta, case_ops, compare_final, golden_cases
+from conftest import REPO, case_meta, case_ops, compare_final, golden_cases
 
 # The restatement uses the same operation order and rounding as the reference's x86 build,
 # so DP results agree to the last few ulps; SP results to float round-off.
@@ -82,3 +82,30 @@ def test_oracle_matches_reference_fresh(n, prec, seed):
     assert np.max(np.abs(a.GetStateVector().astype(np.complex128) - b.GetStateVector())) <= tol
     assert np.max(np.abs(np.asarray(qa) - np.asarray(qb)), initial=0.0) <= (1e-13 if prec == "DP" else 2e-6)
     assert a.perm.map == b.map
+
+
+def _qaoa_extra():
+    import json
+    z = np.load(REPO / "tests" / "golden" / "qaoa_extra.npz")
+    for name in sorted({k.split("/")[0] for k in z.files}):
+        yield name, json.loads(str(z[f"{name}/meta"])), {k.split("/", 1)[1]: z[k] for k in z.files
+                                                         if k.startswith(name + "/")}
+
+
+def test_oracle_weighted_cost_and_histograms_golden():
+    """The C restatement of the weighted cost and the numpy restatement of the histograms
+    against the reference's outputs."""
+    for name, meta, d in _qaoa_extra():
+        n, prec = meta["n"], meta["precision"]
+        diag = oracle.OracleRegister(n, "base", 0, prec)
+        if meta["weighted"]:
+            mx = oracle.oracle_weighted_maxcut_cost(diag, d["adj"])
+        else:
+            mx = oracle.oracle_maxcut_cost(diag, d["adj"].astype(np.int32))
+        assert abs(mx - meta["max_cut"]) <= 1e-12 * max(1, mx), name
+        assert np.max(np.abs(diag.GetStateVector() - d["diag"])) <= 1e-12, name
+        psi = oracle.OracleRegister(n, "", 0, prec)
+        psi.SetStateVector(d["psi"])
+        for k, (mode, width) in enumerate(meta["hists"]):
+            h = oracle.oracle_cost_histogram(psi, diag, mode, meta["max_cut"], width)
+            assert np.max(np.abs(h - d[f"hist{k}"])) <= 1e-12, (name, k)
