@@ -20,6 +20,8 @@ CSRC = ROOT / "csrc"
 INCLUDE = REPO / "include"
 BUILD = ROOT / "_build"
 LIB = PKG_DIR / "libiqsg.so"
+QASM_SRC = ROOT / "qasm" / "iqsg_qasm.cpp"
+QASM = PKG_DIR / "iqsg_qasm"                 # QASM front end over the C++ drop-in header
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -41,8 +43,24 @@ def _stale() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
+    deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
     return any(p.stat().st_mtime > t for p in deps)
+
+
+def build_qasm() -> Path:
+    """Compile the QASM front end (plain C++ over include/iqs_gb300/qureg.hpp and libiqsg.so)."""
+    deps = [QASM_SRC, LIB, *INCLUDE.rglob("*.h"), *INCLUDE.rglob("*.hpp")]
+    if QASM.exists() and all(p.stat().st_mtime <= QASM.stat().st_mtime for p in deps):
+        return QASM
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("g++ not found: needed for the QASM front end")
+    cmd = [cxx, "-std=c++17", "-O2", "-I", str(INCLUDE), str(QASM_SRC), "-L", str(PKG_DIR), "-liqsg",
+           "-Wl,-rpath,$ORIGIN", "-o", str(QASM)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed on {QASM_SRC.name}:\n{r.stdout}\n{r.stderr}")
+    return QASM
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
@@ -76,3 +94,4 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
 if __name__ == "__main__":
     print(build(force=True, verbose=True))
+    print(build_qasm())
