@@ -260,6 +260,12 @@ int iqsg_probability(iqsg_state* h, unsigned pos, double* p);
 int iqsg_expectation_pauli(iqsg_state* h, unsigned k, const unsigned* pos, const unsigned* obs,
                            double* value, double* norm2);
 
+/* State statistics in one read-only pass, as GoogleStats returns them: stats[0] = entropy
+ * -sum p log2 p, stats[1] = -sum log2 p over p > 0 divided by 2^n, stats[2 + i] =
+ * sum p^k * (2^n)^(k-1) / k! for k = 2..10 (p = |amp|^2; FP64 sums in a fixed order).
+ * stats[0] is Entropy(). Replaces Entropy and GoogleStats: src/qureg_utils.cpp:303-450. */
+int iqsg_state_stats(iqsg_state* h, double* stats);
+
 /* sum |amp|^2. ComputeNorm returns its square root: src/qureg_utils.cpp:236-256. */
 int iqsg_norm2(iqsg_state* h, double* out);
 

@@ -879,6 +879,34 @@ int iqsg_weighted_maxcut_cost(iqsg_state* diag, const double* adj, const unsigne
   return fetch_results(diag, 1, max_cut, "iqsg_weighted_maxcut_cost");
 }
 
+int iqsg_state_stats(iqsg_state* h, double* stats) {
+  int st = check_h(h);
+  if (st) return st;
+  if (!stats) return fail(IQSG_EINVAL, "iqsg_state_stats: null output");
+  double* out_dev = h->scratch + kTableSlot;
+  dispatch(h, [&](auto r) {
+    using R = decltype(r);
+    launch_state_stats<R>(h, out_dev);
+  });
+  if ((st = after_launch("iqsg_state_stats"))) return st;
+  double raw[11];
+  if ((st = cuda_status(cudaMemcpyAsync(raw, out_dev, sizeof raw, cudaMemcpyDeviceToHost, h->stream),
+                        "iqsg_state_stats")))
+    return st;
+  if ((st = sync_and_check(h, "iqsg_state_stats"))) return st;
+  // The reference's normalisation (src/qureg_utils.cpp:418-437).
+  const double two2n = (double)h->N, ln2 = std::log(2.0);
+  stats[0] = raw[0] / ln2;
+  stats[1] = raw[1] / ln2 / two2n;
+  double factorial = 1.0;
+  for (int i = 0; i < 9; ++i) {
+    const int k = i + 2;
+    factorial *= (double)k;
+    stats[2 + i] = raw[2 + i] * (std::pow(two2n, (double)(k - 1)) / factorial);
+  }
+  return IQSG_OK;
+}
+
 int iqsg_cost_histogram(iqsg_state* psi, const iqsg_state* diag, int mode, double max_value, double bin_width,
                         double* hist, unsigned num_bins) {
   int st = check_pair(psi, diag, "iqsg_cost_histogram");

@@ -140,6 +140,8 @@ template <typename R> void reduce_max_real(iqsg_state* h);
 // k_costfn.cu: weighted MaxCut cost vector (edge table of (u, v, w) doubles on the device) and
 // cost histograms (out_dev: nbins device doubles; *bad counts values outside the histogram).
 template <typename R> void launch_weighted_cost(iqsg_state* h, const double* edges, unsigned num_edges);
+// k_costfn.cu: 11 state sums (-sum p ln p, -sum ln p over p > 0, sum p^k for k = 2..10) into out_dev.
+template <typename R> void launch_state_stats(iqsg_state* h, double* out_dev);
 template <typename R>
 void launch_cost_hist(iqsg_state* psi, const void* diag, int mode, double max_value, double bin_width, int nbins,
                       double* out_dev, unsigned long long* bad);

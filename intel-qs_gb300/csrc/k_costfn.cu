@@ -1,5 +1,6 @@
-// Cost-function helpers of QAOA on the GPU: the weighted MaxCut cost vector and histograms of
-// |psi|^2 over the cost values (src/qaoa_features.cpp:153-239, :335-540).
+// Cost-function helpers of QAOA on the GPU -- the weighted MaxCut cost vector and histograms of
+// |psi|^2 over the cost values (src/qaoa_features.cpp:153-239, :335-540) -- and the state
+// statistics of Entropy / GoogleStats (src/qureg_utils.cpp:303-450).
 #include "iqsg_internal.cuh"
 
 namespace iqsg {
@@ -90,7 +91,63 @@ __global__ void k_hist_finish(const double* __restrict__ partials, unsigned nblo
   out[j] = t;
 }
 
+constexpr int kStats = 11;  // -sum p ln p, -sum ln p (p > 0), sum p^2 .. sum p^10
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_state_stats(const typename V2<R>::type* __restrict__ psi, uint64_t N,
+                                                          double* __restrict__ partials) {
+  double acc[kStats];
+#pragma unroll
+  for (int k = 0; k < kStats; ++k) acc[k] = 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x) {
+    const typename V2<R>::type a = psi[i];
+    const double p = (double)a.x * a.x + (double)a.y * a.y;
+    if (p != 0.0) {
+      const double l = log(p);
+      acc[0] -= p * l;
+      acc[1] -= l;
+    }
+    double pk = p;
+#pragma unroll
+    for (int k = 2; k < kStats; ++k) {
+      pk *= p;
+      acc[k] += pk;
+    }
+  }
+  __shared__ double red[kThreads / 32][kStats];
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kStats; ++k) {
+    double x = acc[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < kStats) {
+    double t = 0.0;
+    for (unsigned w = 0; w < kThreads / 32; ++w) t += red[w][threadIdx.x];
+    partials[(uint64_t)blockIdx.x * kStats + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_stats_finish(const double* __restrict__ partials, unsigned nblocks, double* __restrict__ out) {
+  const int k = threadIdx.x;
+  if (k >= kStats) return;
+  double t = 0.0;
+  for (unsigned b = 0; b < nblocks; ++b) t += partials[(uint64_t)b * kStats + k];  // fixed order
+  out[k] = t;
+}
+
 }  // namespace
+
+template <typename R>
+void launch_state_stats(iqsg_state* h, double* out_dev) {
+  unsigned blocks = (unsigned)std::min<uint64_t>((h->N + kThreads - 1) / kThreads, (uint64_t)num_sms() * 2);
+  if (blocks * kStats > 2u * kMaxPartials) blocks = 2u * kMaxPartials / kStats;
+  k_state_stats<R><<<blocks, kThreads, 0, h->stream>>>(reinterpret_cast<const typename V2<R>::type*>(h->amps), h->N,
+                                                       h->scratch);
+  k_stats_finish<<<1, 32, 0, h->stream>>>(h->scratch, blocks, out_dev);
+}
 
 template <typename R>
 void launch_weighted_cost(iqsg_state* h, const double* edges, unsigned num_edges) {
@@ -113,6 +170,8 @@ void launch_cost_hist(iqsg_state* psi, const void* diag, int mode, double max_va
   }
 }
 
+template void launch_state_stats<double>(iqsg_state*, double*);
+template void launch_state_stats<float>(iqsg_state*, double*);
 template void launch_weighted_cost<double>(iqsg_state*, const double*, unsigned);
 template void launch_weighted_cost<float>(iqsg_state*, const double*, unsigned);
 template void launch_cost_hist<double>(iqsg_state*, const void*, int, double, double, int, double*, unsigned long long*);

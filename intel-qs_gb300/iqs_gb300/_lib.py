@@ -86,6 +86,7 @@ SIGNATURES = {
     "iqsg_cost_expectation": [_P, _P, C.c_int, _DP],
     "iqsg_maxcut_cost": [_P, _IP, _UP, _IP],
     "iqsg_weighted_maxcut_cost": [_P, _DP, _UP, _DP],
+    "iqsg_state_stats": [_P, _DP],
     "iqsg_cost_histogram": [_P, _P, C.c_int, _D, _D, _DP, _U],
     "iqsg_apply_ops": [_P, C.POINTER(Op), _U, _UP],
     "iqsg_adjoint_ops": [_P, _P, C.POINTER(Op), _U, _DP, _U, _UP],

@@ -74,6 +74,16 @@ class Permutation:
             out |= ((v >> q) & 1) << p
         return out
 
+    @staticmethod
+    def dec2bin(v: int, num_bits: int) -> str:
+        """Bits of v, least significant first (include/permutation.hpp:208-218)."""
+        return "".join("1" if (v >> i) & 1 else "0" for i in range(num_bits))
+
+    def data2program(self, v: int) -> str:
+        """Program-order bit string of data index v: character q is bit map[q] of v
+        (include/permutation.hpp:267-281)."""
+        return "".join("1" if (v >> p) & 1 else "0" for p in self.map)
+
     def GetMapStr(self) -> str:
         return "".join(f" {p}" for p in self.map)
 

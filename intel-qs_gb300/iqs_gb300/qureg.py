@@ -254,6 +254,60 @@ class QubitRegister:
             raise ValueError(f"index {index} out of range")
         self[self.qubit_permutation.program2data_(int(index))] = value
 
+    # ---- state statistics and output formats --------------------------------------------
+    def GoogleStats(self) -> list:
+        """[entropy, average self-information, scaled moments m2..m10] in one pass on the GPU
+        (src/qureg_utils.cpp:349-450)."""
+        self._flush()
+        out = (C.c_double * 11)()
+        check(lib.iqsg_state_stats(self._h, out))
+        return [float(x) for x in out]
+
+    def Entropy(self) -> float:
+        """-sum p log2 p over the amplitudes (src/qureg_utils.cpp:303-346)."""
+        return self.GoogleStats()[0]
+
+    def _norms(self, a: np.ndarray) -> np.ndarray:
+        if self._prec == _lib.COMPLEX_SP:  # std::norm in float
+            return (a.real * a.real + a.imag * a.imag).astype(np.float32)
+        return a.real * a.real + a.imag * a.imag
+
+    def Print(self, x: str, qubits=()) -> None:
+        """Print the qubit map and every amplitude with its program-order basis string and
+        probability, in the reference's format (src/qureg_utils.cpp:461-563; `qubits` is
+        unused there too). Copies the state to the host."""
+        a = self.GetStateVector()
+        p = self._norms(a)
+        perm = self.qubit_permutation
+        lines = [f"qubit permutation: {perm.GetMapStr()}", f"{x}=["]
+        for i in range(a.size):
+            lines.append("\t%-13.8f + i * %-13.8f   %% |%s> p=%f" % (a[i].real, a[i].imag, perm.data2program(i), p[i]))
+        cum = np.cumsum(p)[-1] if a.size else 0.0  # accumulated in the register's precision
+        lines.append("]; %% cumulative probability = %f" % float(cum))
+        print("\n".join(lines), flush=True)
+
+    def ExportAmplitudes(self, ofname: str) -> None:
+        """Append the amplitudes as JSON members "bits" : [re, im, p] to ofname, in the
+        reference's format (src/qureg_utils.cpp:566-657)."""
+        a = self.GetStateVector()
+        p = self._norms(a)
+        perm = self.qubit_permutation
+        body = "".join("\t\t\"%s\" : [%-13.8f, %-13.8f, %f],\n" % (perm.data2program(i), a[i].real, a[i].imag, p[i])
+                       for i in range(a.size))
+        body = body[:-2] + "\n"  # no comma after the last member
+        with open(ofname, "a") as f:
+            f.write("\t\"amplitudes\" :\n\t{\n" + body + "\t}\n")
+
+    def dumpbin(self, fn: str) -> None:
+        """Write the raw amplitudes (data order, the register's complex type) to fn, as the
+        reference's MPI build does on one rank (src/qureg_utils.cpp:661-689)."""
+        import time
+        t0 = time.perf_counter()
+        a = self.GetStateVector()
+        a.tofile(fn)
+        dt = time.perf_counter() - t0
+        print("Dumping state to %s took %f sec (%f MB/s)" % (fn, dt, a.nbytes / max(dt, 1e-12) / 1e6), flush=True)
+
     # ---- statistics ---------------------------------------------------------------------
     def EnableStatistics(self) -> None:
         self.gate_counter = GateCounter(self._n)

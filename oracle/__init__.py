@@ -431,6 +431,21 @@ def oracle_cost_histogram(psi: OracleRegister, diag: OracleRegister, mode: int, 
     return np.bincount(b, weights=p, minlength=nb)[:nb]
 
 
+def oracle_google_stats(reg: OracleRegister) -> list:
+    """GoogleStats (src/qureg_utils.cpp:349-450) restated with numpy: entropy, average
+    self-information and the scaled moments m2..m10 of p = |amp|^2."""
+    a = reg.GetStateVector().astype(np.complex128)
+    p = a.real * a.real + a.imag * a.imag
+    nz = p[p != 0]
+    two2n = float(p.size)
+    out = [float(-np.sum(nz * np.log(nz)) / math.log(2.0)), float(-np.sum(np.log(nz)) / math.log(2.0) / two2n)]
+    fact = 1.0
+    for k in range(2, 11):
+        fact *= k
+        out.append(float(np.sum(p ** k) * (two2n ** (k - 1) / fact)))
+    return out
+
+
 def ref_available() -> bool:
     return REF_LIB.exists()
 
@@ -460,6 +475,8 @@ def rlib() -> C.CDLL:
             "ref_qaoa_maxcut_cost": ([_P, _IP, _U], C.c_int), "ref_qaoa_layer": ([_P, _P, _D], None),
             "ref_qaoa_expectation": ([_P, _P], _D), "ref_qaoa_expectation_sq": ([_P, _P], _D),
             "ref_qaoa_weighted_cost": ([_P, _DP, _U], _D),
+            "ref_entropy": ([_P], _D), "ref_google_stats": ([_P, _DP, C.c_int], C.c_int),
+            "ref_print": ([_P, C.c_char_p], None), "ref_export": ([_P, C.c_char_p], None),
             "ref_qaoa_histogram": ([_P, _P, C.c_int, _D, _D, _DP, C.c_int], C.c_int),
         }
         for name, (args, res) in sigs.items():

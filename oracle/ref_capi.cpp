@@ -5,6 +5,7 @@
 // with the reference's own sources (built into oracle/_ref/, never committed).
 // Every function forwards to exactly one reference method; no arithmetic here.
 #include <complex>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -184,6 +185,25 @@ int ref_qaoa_histogram(RefReg* psi, RefReg* diag, int mode, double max_value, do
   });
   return len;
 }
+double ref_entropy(RefReg* h) {
+  double r = 0;
+  DISPATCH(h, r = q->Entropy());
+  return r;
+}
+int ref_google_stats(RefReg* h, double* out, int cap) {
+  int len = 0;
+  DISPATCH(h, {
+    std::vector<double> v = q->GoogleStats();
+    len = (int)v.size();
+    for (int i = 0; i < len && i < cap; ++i) out[i] = v[i];
+  });
+  return len;
+}
+void ref_print(RefReg* h, const char* x) {
+  DISPATCH(h, q->Print(std::string(x), std::vector<std::size_t>()));
+  fflush(stdout);
+}
+void ref_export(RefReg* h, const char* fname) { DISPATCH(h, q->ExportAmplitudes(std::string(fname))); }
 double ref_qaoa_expectation_sq(RefReg* psi, RefReg* diag) {
   double r = 0;
   DISPATCH(psi, r = iqs::qaoa::GetExpectationValueSquaredFromCostFunction(*q, *R<T>(diag)));

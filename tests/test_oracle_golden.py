@@ -109,3 +109,16 @@ def test_oracle_weighted_cost_and_histograms_golden():
         for k, (mode, width) in enumerate(meta["hists"]):
             h = oracle.oracle_cost_histogram(psi, diag, mode, meta["max_cut"], width)
             assert np.max(np.abs(h - d[f"hist{k}"])) <= 1e-12, (name, k)
+
+
+def test_oracle_google_stats_golden():
+    import json
+    z = np.load(REPO / "tests" / "golden" / "state_io.npz")
+    for name in sorted({k.split("/")[0] for k in z.files}):
+        meta = json.loads(str(z[f"{name}/meta"]))
+        r = oracle.OracleRegister(meta["n"], "base", 0, meta["precision"])
+        r.SetStateVector(z[f"{name}/init"])
+        want = z[f"{name}/stats"]
+        got = np.asarray(oracle.oracle_google_stats(r))
+        tol = 1e-12 if meta["precision"] == "DP" else 1e-5
+        assert np.max(np.abs(got - want) / np.maximum(1.0, np.abs(want))) <= tol, name
