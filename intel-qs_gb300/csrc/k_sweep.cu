@@ -574,7 +574,18 @@ extern "C" int iqsg_adjoint_ops(iqsg_state* psi, iqsg_state* lam, const iqsg_op*
     if ((st = tile_schedule(psi, lam, ops, count, kt, kmax, dgrad, sweeps))) return st;
   } else {
     SweepBuilder b(psi, lam, dgrad, kmax);
-    for (unsigned i = 0; i < count; ++i) queue_op(b, ops[i]);
+    for (unsigned i = 0; i < count; ++i) {
+      // A gradient op followed by its excitation-preserving gate on the same pair becomes one
+      // operation (one pass over each quad of psi and lambda).
+      const iqsg_op& g = ops[i];
+      if (i + 1 < count && g.kind == IQSG_OP_GRAD2 && ops[i + 1].kind == IQSG_OP_2Q && ops[i + 1].t0 == g.t0 &&
+          ops[i + 1].t1 == g.t1 && SweepBuilder::is_excitation(g.m) && SweepBuilder::is_excitation(ops[i + 1].m)) {
+        b.add_grad_and_excitation(g.t0, g.t1, g.m, ops[i + 1].m, (unsigned)g.value);
+        ++i;
+        continue;
+      }
+      queue_op(b, g);
+    }
     b.flush();
     if (sweeps) *sweeps = b.launched();
   }

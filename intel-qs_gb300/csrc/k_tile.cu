@@ -98,7 +98,9 @@ __device__ __forceinline__ void tile_phase(const TileParams& P, const TilePhase&
 #pragma unroll 1
       for (unsigned o = ph.op0; o < (unsigned)ph.op0 + ph.nops; ++o) {
         const SweepOp op = P.ops[o];
-        if (op.kind == SW_GRAD1 || op.kind == SW_GRAD2 || op.kind == SW_GRADEXC) {
+        if (op.kind == SW_EXCADJ) {
+          acc[op.value] += excadj_op<R, K>(P.ent, op, v, w, idx, tm);
+        } else if (op.kind == SW_GRAD1 || op.kind == SW_GRAD2 || op.kind == SW_GRADEXC) {
           acc[op.value] += grad_op<R, K>(P.ent, op, v, w, idx);
         } else {
           apply_op<A, K>(P.ent, op, v, idx, tm);
@@ -263,6 +265,7 @@ unsigned entries_of(const SweepOp& op) {
     case SW_PHASE: return 1;
     case SW_U2: case SW_SWAPLIKE: case SW_GRAD1: return 4;
     case SW_EXC: case SW_GRADEXC: return 6;
+    case SW_EXCADJ: return 12;
     default: return 16;  // SW_U4, SW_GRAD2
   }
 }
@@ -305,7 +308,8 @@ class TileAssembler : public SweepSink {
     for (unsigned o = 0; o < S.nops; ++o) {
       SweepOp op = S.ops[o];
       op.ent = (uint16_t)(op.ent + nent_);
-      if (op.kind == SW_GRAD1 || op.kind == SW_GRAD2 || op.kind == SW_GRADEXC) op.value += map_.nslots;
+      if (op.kind == SW_GRAD1 || op.kind == SW_GRAD2 || op.kind == SW_GRADEXC || op.kind == SW_EXCADJ)
+        op.value += map_.nslots;
       P_.ops[nops_++] = op;
     }
     std::copy(S.ent, S.ent + used, P_.ent + nent_);

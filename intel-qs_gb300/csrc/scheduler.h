@@ -213,6 +213,25 @@ class SweepBuilder {
     P_.ops[P_.nops++] = op;
   }
 
+  // Adjoint mode: a parameterised excitation-preserving gate undone in one operation: the
+  // gradient sum for M (4x4, rows 2*b(t0) + b(t1)), then the 4x4 gate g on both vectors.
+  // Both matrices must have the excitation layout (is_excitation).
+  void add_grad_and_excitation(unsigned t0, unsigned t1, const double* M, const double* g, unsigned param) {
+    double w[24];
+    excitation_entries(t0, t1, M, w);
+    excitation_entries(t0, t1, g, w + 12);
+    const unsigned lo = std::min(t0, t1), hi = std::max(t0, t1);
+    reserve({lo, hi}, 1, 12, 1);
+    SweepOp op{};
+    op.kind = SW_EXCADJ;
+    op.j0 = (uint8_t)slot(lo);
+    op.j1 = (uint8_t)slot(hi);
+    op.value = map_.nslots;
+    map_.param[map_.nslots++] = param;
+    op.ent = add_entries(w, 12);
+    P_.ops[P_.nops++] = op;
+  }
+
   // Adjoint mode: add Im <lam|M|psi> on the target positions into grad[param]; M is 2x2
   // (one target) or 4x4 (rows 2*b(t0) + b(t1)).
   void add_grad(unsigned ntargets, unsigned t0, unsigned t1, const double* m, unsigned param) {

@@ -34,6 +34,8 @@ enum SweepKind : uint8_t {
   SW_GRADEXC = 7,   // adjoint sweeps only: Im <w|M|v> for M with the SW_EXC layout
   SW_CZSHIFT = 8,   // amp *= (-1)^popcount(idx & (idx >> j0) & mask): the product of CZ(a, a + j0)
                     // over the bits a of mask (exact sign flips)
+  SW_EXCADJ = 9,    // adjoint sweeps only: SW_GRADEXC with entries 0-5, then SW_EXC with entries
+                    // 6-11 on both vectors, quad by quad (one parameterised excitation gate undone)
 };
 
 enum SweepFlags : uint8_t {
@@ -426,6 +428,51 @@ __device__ __forceinline__ R grad_exc(const SweepEntry* E, const SweepOp& op, co
   return c;
 }
 
+template <typename R, int K, int JLO, int JHI>
+__device__ __forceinline__ R excadj(const SweepEntry* E, const SweepOp& op, typename NativeArith<R>::VT* v,
+                                    typename NativeArith<R>::VT* w, const uint64_t* idx, unsigned& tm) {
+  using A = NativeArith<R>;
+  constexpr int G = 1 << K, BL = 1 << JLO, BH = 1 << JHI;
+  const SweepEntry* m = E + op.ent;
+  const SweepEntry* g = m + 6;
+  R c = 0;
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    if (s & (BH | BL)) continue;
+    if ((idx[s] & op.mask) != op.mask) continue;
+    tm |= (1u << s) | (1u << (s | BL)) | (1u << (s | BH)) | (1u << (s | BH | BL));
+    const typename A::VT a = v[s | BL], b = v[s | BH], la = w[s | BL], lb = w[s | BH];
+    c += im_cdot<R>(w[s], A::mul(m[0], v[s])) + im_cdot<R>(la, A::row(m[1], m[2], a, b)) +
+         im_cdot<R>(lb, A::row(m[3], m[4], a, b)) + im_cdot<R>(w[s | BH | BL], A::mul(m[5], v[s | BH | BL]));
+    v[s] = A::mul(g[0], v[s]);
+    v[s | BL] = A::row(g[1], g[2], a, b);
+    v[s | BH] = A::row(g[3], g[4], a, b);
+    v[s | BH | BL] = A::mul(g[5], v[s | BH | BL]);
+    w[s] = A::mul(g[0], w[s]);
+    w[s | BL] = A::row(g[1], g[2], la, lb);
+    w[s | BH] = A::row(g[3], g[4], la, lb);
+    w[s | BH | BL] = A::mul(g[5], w[s | BH | BL]);
+  }
+  return c;
+}
+
+template <typename R, int K>
+__device__ __forceinline__ R excadj_op(const SweepEntry* E, const SweepOp& op, typename NativeArith<R>::VT* v,
+                                       typename NativeArith<R>::VT* w, const uint64_t* idx, unsigned& tm) {
+  if constexpr (K >= 2) {
+    const int a = op.j0, b = op.j1;
+#define IQSG_EXCADJ_CASE(X, Y)                                      \
+  if (a == X && b == Y) {                                           \
+    if constexpr (K > (X > Y ? X : Y)) return excadj<R, K, X, Y>(E, op, v, w, idx, tm); \
+  }
+    IQSG_EXCADJ_CASE(0, 1) IQSG_EXCADJ_CASE(1, 0) IQSG_EXCADJ_CASE(0, 2) IQSG_EXCADJ_CASE(2, 0)
+    IQSG_EXCADJ_CASE(1, 2) IQSG_EXCADJ_CASE(2, 1) IQSG_EXCADJ_CASE(0, 3) IQSG_EXCADJ_CASE(3, 0)
+    IQSG_EXCADJ_CASE(1, 3) IQSG_EXCADJ_CASE(3, 1) IQSG_EXCADJ_CASE(2, 3) IQSG_EXCADJ_CASE(3, 2)
+#undef IQSG_EXCADJ_CASE
+  }
+  return R(0);
+}
+
 template <typename R, int K>
 __device__ __forceinline__ R grad_op(const SweepEntry* E, const SweepOp& op, const typename NativeArith<R>::VT* v,
                                      const typename NativeArith<R>::VT* w, const uint64_t* idx) {
@@ -463,7 +510,9 @@ __device__ __forceinline__ void run_ops_dual(const SweepParams& P, typename Nati
 #pragma unroll 1
   for (unsigned o = 0; o < P.nops; ++o) {
     const SweepOp op = P.ops[o];
-    if (op.kind == SW_GRAD1 || op.kind == SW_GRAD2 || op.kind == SW_GRADEXC) {
+    if (op.kind == SW_EXCADJ) {
+      acc[op.value] += excadj_op<R, K>(P.ent, op, v, w, idx, tm);
+    } else if (op.kind == SW_GRAD1 || op.kind == SW_GRAD2 || op.kind == SW_GRADEXC) {
       acc[op.value] += grad_op<R, K>(P.ent, op, v, w, idx);
     } else {
       apply_op<A, K>(P.ent, op, v, idx, tm);
