@@ -9,6 +9,7 @@ from conftest import REPO
 def qasm(text):
     sys.path.insert(0, str(REPO / "intel-qs_gb300"))
     import iqsg_build
+    iqsg_build.build()  # no-op when libiqsg.so is current
     exe = iqsg_build.build_qasm()
     return subprocess.run([str(exe)], input=text, capture_output=True, text=True, timeout=60)
 
