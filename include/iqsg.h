@@ -62,6 +62,10 @@ int iqsg_version(void);
 
 /* ---- lifecycle ------------------------------------------------------------------------ */
 
+/* Devices: a register lives on the device that is current (cudaSetDevice) when it is created,
+ * and every call on it must be made with that device current, as with any CUDA runtime
+ * object. Several devices may be used from one process this way. */
+
 /* Allocate a register of num_qubits qubits on the current CUDA device and zero it.
  * stream: a cudaStream_t to queue work on, or NULL for a stream owned by the register.
  * Replaces QubitRegister(n, style, base, tmp) allocation: src/qureg_init.cpp:149-188. */

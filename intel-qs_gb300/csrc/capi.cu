@@ -30,14 +30,21 @@ int cuda_status(cudaError_t e, const char* what) {
   return fail(code, "%s: %s", what, cudaGetErrorString(e));
 }
 
+int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+  return dev;
+}
+
 int num_sms() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+  static int sms[kMaxDevices] = {};  // per device, filled on first use
+  const int dev = current_device();
+  if (!sms[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+    sms[dev] = v;
   }
-  return sms;
+  return sms[dev];
 }
 
 unsigned grid_for(uint64_t work, int per_thread) {

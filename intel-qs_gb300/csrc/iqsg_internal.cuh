@@ -48,6 +48,9 @@ int fail(int code, const char* fmt, ...);
 int cuda_status(cudaError_t e, const char* what);
 // Grid size for a grid-stride loop over `work` items, `per_thread` items per thread.
 unsigned grid_for(uint64_t work, int per_thread);
+// Launch facts cached per device (the device current at the call).
+constexpr int kMaxDevices = 64;
+int current_device();
 int num_sms();
 // Wait for the register's stream and report a device error word left by a bounded wait.
 int sync_and_check(iqsg_state* h, const char* what);

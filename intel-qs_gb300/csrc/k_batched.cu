@@ -122,6 +122,8 @@ __device__ __forceinline__ void apply2(const Mat<R>& M, CXb<R>& a, CXb<R>& b) {
   b = o1;
 }
 
+constexpr int kGroupsInFlight = 2;
+
 // Forward: RZ then RY on qubits q0 .. q0+W-1 of one layer in a single pass over groups of 2^W
 // amplitudes (the W qubits' index bits), in qubit order; the layer's CZ ladder rides on the
 // pass that holds the last qubit.
@@ -134,31 +136,47 @@ __device__ __forceinline__ void fwd_chunk(typename V2<R>::type* __restrict__ psi
 #pragma unroll
   for (int k = 0; k < W; ++k) M[k] = ry_rz<R>(prm_l[2 * (q0 + k) + 1], prm_l[2 * (q0 + k)]);
   const uint64_t groups = N >> W, lowmask = (uint64_t(1) << q0) - 1;
-  for (uint64_t p = threadIdx.x; p < groups; p += blockDim.x) {
-    const uint64_t base = (p & lowmask) | ((p >> q0) << (q0 + W));
-    CXb<R> a[G];
+  // kGroupsInFlight groups per iteration: all their loads are issued before any arithmetic,
+  // so a thread keeps that many groups' worth of loads in flight.
+  for (uint64_t p0 = threadIdx.x; p0 < groups; p0 += kGroupsInFlight * blockDim.x) {
+    uint64_t base[kGroupsInFlight];
+    bool ok[kGroupsInFlight];
+    CXb<R> a[kGroupsInFlight][G];
 #pragma unroll
-    for (int j = 0; j < G; ++j) {
-      const V v = psi[base | ((uint64_t)j << q0)];
-      a[j].re = v.x;
-      a[j].im = v.y;
+    for (int u = 0; u < kGroupsInFlight; ++u) {
+      const uint64_t p = p0 + (uint64_t)u * blockDim.x;
+      ok[u] = p < groups;
+      base[u] = (p & lowmask) | ((p >> q0) << (q0 + W));
+#pragma unroll
+      for (int j = 0; j < G; ++j) {
+        V v;
+        v.x = 0;
+        v.y = 0;
+        if (ok[u]) v = psi[base[u] | ((uint64_t)j << q0)];
+        a[u][j].re = v.x;
+        a[u][j].im = v.y;
+      }
     }
 #pragma unroll
-    for (int k = 0; k < W; ++k)
+    for (int u = 0; u < kGroupsInFlight; ++u) {
+      if (!ok[u]) continue;
 #pragma unroll
-      for (int j = 0; j < G; ++j)
-        if (!(j & (1 << k))) apply2(M[k], a[j], a[j | (1 << k)]);
+      for (int k = 0; k < W; ++k)
 #pragma unroll
-    for (int j = 0; j < G; ++j) {
-      const uint64_t i = base | ((uint64_t)j << q0);
-      if (last && (__popcll(i & (i >> 1) & ladder) & 1)) {
-        a[j].re = -a[j].re;
-        a[j].im = -a[j].im;
+        for (int j = 0; j < G; ++j)
+          if (!(j & (1 << k))) apply2(M[k], a[u][j], a[u][j | (1 << k)]);
+#pragma unroll
+      for (int j = 0; j < G; ++j) {
+        const uint64_t i = base[u] | ((uint64_t)j << q0);
+        if (last && (__popcll(i & (i >> 1) & ladder) & 1)) {
+          a[u][j].re = -a[u][j].re;
+          a[u][j].im = -a[u][j].im;
+        }
+        V o;
+        o.x = a[u][j].re;
+        o.y = a[u][j].im;
+        psi[i] = o;
       }
-      V o;
-      o.x = a[j].re;
-      o.y = a[j].im;
-      psi[i] = o;
     }
   }
 }

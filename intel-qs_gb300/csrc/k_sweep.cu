@@ -398,15 +398,17 @@ template <typename R, bool DF, int K>
 void launch_bulk(iqsg_state* h, const SweepParams& P, const TileGeom& g) {
   using V = typename V2<R>::type;
   const size_t smem = (size_t)kTmaStages * (size_t(256) << K) * sizeof(V);
-  static int blocks_per_sm = -1;  // per instantiation
-  if (blocks_per_sm < 0) {
+  static int per_device[kMaxDevices] = {};  // per instantiation and device; 0 = not configured yet
+  const int dev = current_device();
+  if (!per_device[dev]) {
     cudaFuncSetAttribute(k_sweep_bulk<R, DF, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_sweep_bulk<R, DF, K>, kTmaThreads, smem) != cudaSuccess ||
         b < 1)
       b = 1;
-    blocks_per_sm = b;
+    per_device[dev] = b;
   }
+  const int blocks_per_sm = per_device[dev];
   const uint64_t ntiles = h->N >> (K + 8);
   uint64_t grid = (uint64_t)num_sms() * (uint64_t)blocks_per_sm;
   if (grid > ntiles) grid = ntiles;

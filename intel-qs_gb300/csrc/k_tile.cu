@@ -401,11 +401,12 @@ int launch_tile(iqsg_state* h, iqsg_state* lam, const TileAssembler& a, double* 
   const bool dual = lam != nullptr;
   const size_t smem = tile_smem<V>(P.kt, P.nhi, dual);
   const void* fn = dual ? (const void*)k_tile_adj<R> : (const void*)k_tile<R>;
-  static size_t configured[2] = {0, 0};  // largest dynamic smem set per kernel of this R
-  if (smem > 48 * 1024 && smem > configured[dual]) {
+  static size_t configured[kMaxDevices][2] = {};  // largest dynamic smem set per device and kernel of this R
+  const int dev = current_device();
+  if (smem > 48 * 1024 && smem > configured[dev][dual]) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "tile pass: shared memory");
-    configured[dual] = smem;
+    configured[dev][dual] = smem;
   }
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTileThreads, smem) != cudaSuccess || per_sm < 1)
