@@ -130,7 +130,8 @@ class ClockSampler:
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
-        self.path = REPO / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        import tempfile
+        self.path = Path(tempfile.gettempdir()) / f"iqsg_bench_clocks_{os.getpid()}.csv"
 
     def start(self):
         try:
