@@ -210,7 +210,7 @@ __device__ __forceinline__ void op_u2(const SweepEntry* E, const SweepOp& op, ty
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & B) continue;
-    if ((idx[s] & op.mask) != op.mask) continue;
+    if (op.mask && (idx[s] & op.mask) != op.mask) continue;
     typename A::VT a = v[s], b = v[s | B];
     tm |= (1u << s) | (1u << (s | B));
     if (op.flags & SF_X) {
@@ -231,7 +231,7 @@ __device__ __forceinline__ void op_u4(const SweepEntry* E, const SweepOp& op, ty
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & (BH | BL)) continue;
-    if ((idx[s] & op.mask) != op.mask) continue;
+    if (op.mask && (idx[s] & op.mask) != op.mask) continue;
     const typename A::VT q[4] = {v[s], v[s | BL], v[s | BH], v[s | BH | BL]};
     tm |= (1u << s) | (1u << (s | BL)) | (1u << (s | BH)) | (1u << (s | BH | BL));
     v[s] = A::row4(m, q);
@@ -249,7 +249,7 @@ __device__ __forceinline__ void op_swaplike(const SweepEntry* E, const SweepOp& 
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & (BH | BL)) continue;
-    if ((idx[s] & op.mask) != op.mask) continue;
+    if (op.mask && (idx[s] & op.mask) != op.mask) continue;
     typename A::VT a = v[s | BL], b = v[s | BH];
     tm |= (1u << (s | BL)) | (1u << (s | BH));
     if (op.flags & SF_X) {
@@ -270,7 +270,7 @@ __device__ __forceinline__ void op_exc(const SweepEntry* E, const SweepOp& op, t
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & (BH | BL)) continue;
-    if ((idx[s] & op.mask) != op.mask) continue;
+    if (op.mask && (idx[s] & op.mask) != op.mask) continue;
     tm |= (1u << s) | (1u << (s | BL)) | (1u << (s | BH)) | (1u << (s | BH | BL));
     const typename A::VT a = v[s | BL], b = v[s | BH];
     v[s] = A::mul(m[0], v[s]);
@@ -385,7 +385,7 @@ __device__ __forceinline__ R grad1(const SweepEntry* E, const SweepOp& op, const
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & B) continue;
-    if ((idx[s] & op.mask) != op.mask) continue;
+    if (op.mask && (idx[s] & op.mask) != op.mask) continue;
     const typename A::VT a = v[s], b = v[s | B];
     c += im_cdot<R>(w[s], A::row(m[0], m[1], a, b)) + im_cdot<R>(w[s | B], A::row(m[2], m[3], a, b));
   }
@@ -402,7 +402,7 @@ __device__ __forceinline__ R grad2(const SweepEntry* E, const SweepOp& op, const
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & (BH | BL)) continue;
-    if ((idx[s] & op.mask) != op.mask) continue;
+    if (op.mask && (idx[s] & op.mask) != op.mask) continue;
     const typename A::VT q[4] = {v[s], v[s | BL], v[s | BH], v[s | BH | BL]};
     c += im_cdot<R>(w[s], A::row4(m, q)) + im_cdot<R>(w[s | BL], A::row4(m + 4, q)) +
          im_cdot<R>(w[s | BH], A::row4(m + 8, q)) + im_cdot<R>(w[s | BH | BL], A::row4(m + 12, q));
@@ -420,7 +420,7 @@ __device__ __forceinline__ R grad_exc(const SweepEntry* E, const SweepOp& op, co
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & (BH | BL)) continue;
-    if ((idx[s] & op.mask) != op.mask) continue;
+    if (op.mask && (idx[s] & op.mask) != op.mask) continue;
     const typename A::VT a = v[s | BL], b = v[s | BH];
     c += im_cdot<R>(w[s], A::mul(m[0], v[s])) + im_cdot<R>(w[s | BL], A::row(m[1], m[2], a, b)) +
          im_cdot<R>(w[s | BH], A::row(m[3], m[4], a, b)) + im_cdot<R>(w[s | BH | BL], A::mul(m[5], v[s | BH | BL]));
@@ -439,7 +439,7 @@ __device__ __forceinline__ R excadj(const SweepEntry* E, const SweepOp& op, type
 #pragma unroll
   for (int s = 0; s < G; ++s) {
     if (s & (BH | BL)) continue;
-    if ((idx[s] & op.mask) != op.mask) continue;
+    if (op.mask && (idx[s] & op.mask) != op.mask) continue;
     tm |= (1u << s) | (1u << (s | BL)) | (1u << (s | BH)) | (1u << (s | BH | BL));
     const typename A::VT a = v[s | BL], b = v[s | BH], la = w[s | BL], lb = w[s | BH];
     c += im_cdot<R>(w[s], A::mul(m[0], v[s])) + im_cdot<R>(la, A::row(m[1], m[2], a, b)) +
