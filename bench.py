@@ -475,7 +475,8 @@ def qft_brick_section(n: int = 30, layers: int = 40) -> dict:
     return out
 
 
-def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int = 4, grad_steps: int = 10) -> dict:
+def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int = 4, grad_steps: int = 10,
+                    tile_qubits: int = 0) -> dict:
     """Open XXZ chain (31 bonds at n = 32, J ~ U[0.5, 1.5] seed 7, delta = 0.8, dt = 0.05) from
     the Neel state: 100 Strang steps in ComplexSP with the 31 bond correlators, then the
     energy sum_b <Z_b Z_{b+1}> and its gradient w.r.t. every J_b by the checkpointed adjoint;
@@ -496,7 +497,7 @@ def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int
         if (2 + len(range(c, steps, c))) * vec + (16 << 30) <= free:
             every = c
             break
-    chain = XXZChain(n, J, steps=steps, precision="SP", checkpoint_every=None)
+    chain = XXZChain(n, J, steps=steps, precision="SP", checkpoint_every=None, tile_qubits=tile_qubits)
     gates = sum(len(b) for b, _ in chain.layers())
     chain.psi.synchronize()
     t0 = time.perf_counter()
@@ -507,7 +508,7 @@ def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int
     chain.sweeps_forward = 0
     del chain
     gchain = XXZChain(n, J, steps=grad_steps, precision="SP",
-                      checkpoint_every=every if (every and grad_steps > every) else None)
+                      checkpoint_every=every if (every and grad_steps > every) else None, tile_qubits=tile_qubits)
     gchain.forward()
     gchain.psi.synchronize()
     t0 = time.perf_counter()
@@ -852,6 +853,8 @@ def main() -> None:
                     help="run one section alone and print its JSON (a profiling entry point; not the bench line)")
     ap.add_argument("--section-qubits", type=int, default=0, help="with --only: register size of the section")
     ap.add_argument("--section-steps", type=int, default=0, help="with --only trotter: Strang steps")
+    ap.add_argument("--tile-qubits", type=int, default=0,
+                    help="with --only trotter: run the ComplexSP chain as shared-memory tile passes of this size")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -877,7 +880,7 @@ def run_section(args) -> None:
         out = qft_brick_section(n=q or 30)
     else:
         out = trotter_section(n=q or 32, steps=st or 100, n_dp=(q + 1) if q else 33, steps_dp=4,
-                              grad_steps=min(st or 10, 10))
+                              grad_steps=min(st or 10, 10), tile_qubits=args.tile_qubits)
     print(json.dumps({"section": args.only, **out}), flush=True)
 
 
