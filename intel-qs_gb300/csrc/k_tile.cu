@@ -39,7 +39,8 @@ struct TilePhase {
   uint8_t K;
   uint8_t lpos[4];     // slot j <-> local bit lpos[j]
   uint8_t lsorted[4];  // local bits ascending
-  uint8_t pad[3];
+  uint8_t needs_idx;   // some operation reads the data index (controls, phases, CZ runs)
+  uint8_t pad[2];
   uint16_t op0, nops;
 };
 
@@ -69,6 +70,16 @@ __device__ __forceinline__ void tile_phase(const TileParams& P, const TilePhase&
   constexpr int G = 1 << K;
   const uint32_t groups = T >> K;
   const uint32_t lowmask = (1u << P.tl) - 1;
+  const bool need_idx = ph.needs_idx != 0;
+  uint32_t off[G];  // local offset of each slot, the same for every group of the phase
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if (s & (1 << j)) o |= 1u << ph.lpos[j];
+    off[s] = o;
+  }
   for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
     uint32_t lb = g;
 #pragma unroll
@@ -78,12 +89,9 @@ __device__ __forceinline__ void tile_phase(const TileParams& P, const TilePhase&
     typename A::VT v[G], w[DUAL ? G : 1];
 #pragma unroll
     for (int s = 0; s < G; ++s) {
-      uint32_t o = lb;
-#pragma unroll
-      for (int j = 0; j < K; ++j)
-        if (s & (1 << j)) o |= 1u << ph.lpos[j];
+      const uint32_t o = lb | off[s];
       loc[s] = o;
-      idx[s] = base | (o & lowmask) | hiexp[o >> P.tl];
+      idx[s] = need_idx ? (base | (o & lowmask) | hiexp[o >> P.tl]) : 0;
       const V a = sm[swz<V>(o)];
       v[s].re = a.x;
       v[s].im = a.y;
@@ -298,6 +306,8 @@ class TileAssembler : public SweepSink {
     std::sort(ph.lsorted, ph.lsorted + S.K);
     ph.op0 = (uint16_t)nops_;
     ph.nops = (uint16_t)S.nops;
+    for (unsigned o = 0; o < S.nops; ++o)
+      if (S.ops[o].mask || S.ops[o].kind == SW_PHASE || S.ops[o].kind == SW_CZSHIFT) ph.needs_idx = 1;
     unsigned used = 0;
     for (unsigned o = 0; o < S.nops; ++o) used = std::max(used, (unsigned)S.ops[o].ent + entries_of(S.ops[o]));
     if (overflow || P_.nphases + 1 > (unsigned)kTileMaxPhases || nops_ + S.nops > (unsigned)kTileMaxOps ||
