@@ -13,6 +13,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -107,6 +108,17 @@ class Permutation {
     std::size_t out = 0;
     for (std::size_t q = 0; q < map.size(); ++q) out |= ((v >> map[q]) & 1u) << q;
     return out;
+  }
+  // Program-order bit string of data index v: character q is bit map[q] (include/permutation.hpp:267-281).
+  std::string data2program(std::size_t v) const {
+    std::string s(map.size(), '0');
+    for (std::size_t q = 0; q < map.size(); ++q) s[q] = ((v >> map[q]) & 1u) ? '1' : '0';
+    return s;
+  }
+  std::string GetMapStr() const {
+    std::string s;
+    for (auto p : map) s += " " + std::to_string(p);
+    return s;
   }
 };
 
@@ -277,6 +289,18 @@ class QubitRegister {
     check_status(iqsg_apply_diag_2q(h_, p1, p2, op.m));
   }
 
+  // The same diagonal as ApplyDiag, not counted as a gate (src/qureg_applydiag.cpp:17-51).
+  void ApplyDiagSimp(unsigned qubit_1, unsigned qubit_2, const TM4x4<Type>& m) {
+    std::unique_ptr<GateCounter> keep(counter_.release());
+    try {
+      ApplyDiag(qubit_1, qubit_2, m);
+    } catch (...) {
+      counter_.reset(keep.release());
+      throw;
+    }
+    counter_.reset(keep.release());
+  }
+
   // ---- named one-qubit gates (src/qureg_apply1qubitgate.cpp:277-501) ----
   void ApplyRotationX(unsigned q, BaseType t) {
     TM2x2<Type> m;
@@ -429,6 +453,42 @@ class QubitRegister {
     const double e = qubits.size() > 1 ? v : 1.0 - n2 + v;  // single factor: 1 - 2 P(1), as the reference
     return coeff * (BaseType)e;
   }
+  // ---- state statistics and formats (src/qureg_utils.cpp:303-657) ----
+  std::vector<double> GoogleStats() {
+    ApplyFusedGates();
+    std::vector<double> v(11);
+    check_status(iqsg_state_stats(h_, v.data()));
+    return v;
+  }
+  double Entropy() { return GoogleStats()[0]; }
+  void Print(std::string x, std::vector<std::size_t> /*qubits: unused, as in the reference*/ = {}) {
+    const std::vector<Type> a = GetStateVector();
+    BaseType cum = 0;
+    std::printf("qubit permutation: %s\n", perm_.GetMapStr().c_str());
+    std::printf("%s=[\n", x.c_str());
+    for (std::size_t i = 0; i < a.size(); ++i) {
+      std::printf("\t%-13.8lf + i * %-13.8lf   %% |%s> p=%lf\n", (double)a[i].real(), (double)a[i].imag(),
+                  perm_.data2program(i).c_str(), (double)std::norm(a[i]));
+      cum += std::norm(a[i]);
+    }
+    std::printf("]; %% cumulative probability = %lf\n", (double)cum);
+  }
+  void ExportAmplitudes(std::string ofname) {
+    const std::vector<Type> a = GetStateVector();
+    std::string body;
+    char line[512];
+    for (std::size_t i = 0; i < a.size(); ++i) {
+      std::snprintf(line, sizeof line, "\t\t\"%s\" : [%-13.8lf, %-13.8lf, %lf],\n", perm_.data2program(i).c_str(),
+                    (double)a[i].real(), (double)a[i].imag(), (double)std::norm(a[i]));
+      body += line;
+    }
+    if (body.size() >= 2) body = body.substr(0, body.size() - 2) + "\n";
+    std::FILE* f = std::fopen(ofname.c_str(), "a");
+    if (!f) throw std::runtime_error("ExportAmplitudes: cannot open " + ofname);
+    std::fprintf(f, "\t\"amplitudes\" :\n\t{\n%s\t}\n", body.c_str());
+    std::fclose(f);
+  }
+
   BaseType ExpectationValueX(unsigned q, BaseType c = 1.) { return ev({q}, {1}, c); }
   BaseType ExpectationValueY(unsigned q, BaseType c = 1.) { return ev({q}, {2}, c); }
   BaseType ExpectationValueZ(unsigned q, BaseType c = 1.) { return ev({q}, {3}, c); }

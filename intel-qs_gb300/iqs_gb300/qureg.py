@@ -442,6 +442,14 @@ class QubitRegister:
             check(lib.iqsg_apply_2q(self._h, ph, pl, dptr(m32)))
         self._count2(qubit_high, qubit_low)
 
+    def ApplyDiagSimp(self, qubit_1: int, qubit_2: int, m) -> None:
+        """The same diagonal as ApplyDiag, not counted as a gate (src/qureg_applydiag.cpp:17-51)."""
+        counter, self.gate_counter = self.gate_counter, None
+        try:
+            self.ApplyDiag(qubit_1, qubit_2, m)
+        finally:
+            self.gate_counter = counter
+
     def ApplyDiag(self, qubit_1: int, qubit_2: int, m) -> None:
         """src/qureg_applydiag.cpp:55-227: amp *= m[k][k], k = 2 b(qubit_1) + b(qubit_2)."""
         a = np.asarray(m, dtype=np.complex128)

@@ -13,3 +13,5 @@ def test_cpp_header_compiles(tmp_path):
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(REPO / "include"), str(src)], check=True)
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(REPO / "include"),
                     str(REPO / "tests" / "cpp" / "shim_driver.cpp")], check=True)
+    subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(REPO / "include"),
+                    str(REPO / "tests" / "cpp" / "qaoa_driver.cpp")], check=True)

@@ -90,3 +90,42 @@ def test_cpp_header_matches_oracle(driver, tmp_path, fusion):
     assert maps == ref.perm.map
     state = np.fromfile(tmp_path / "s.bin", dtype=np.complex128)
     assert np.max(np.abs(state - ref.GetStateVector())) <= TOL_DP
+
+
+def test_cpp_qaoa_header_and_formats(tmp_path, capsys):
+    """include/iqs_gb300/qaoa_features.hpp and the statistics / Print of the C++ register
+    against the reference's outputs (tests/golden/qaoa_extra.npz) and the oracle."""
+    import json
+    import iqs_gb300 as iqs
+    libdir = REPO / "intel-qs_gb300" / "iqs_gb300"
+    exe = tmp_path / "qaoa_driver"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", str(REPO / "include"), str(REPO / "tests" / "cpp" / "qaoa_driver.cpp"),
+                    "-L", str(libdir), "-liqsg", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, check=True)
+    vals = {}
+    text = []
+    for line in r.stdout.splitlines():
+        parts = line.split(" ")
+        if len(parts) == 2 and parts[0] in ("max", "cost4", "cost36", "expect", "h0", "h1", "h2", "stat"):
+            vals.setdefault(parts[0], []).append(float(parts[1]))
+        else:
+            text.append(line)
+    z = np.load(REPO / "tests" / "golden" / "qaoa_extra.npz")
+    meta = json.loads(str(z["w_ring6/meta"]))
+    assert abs(vals["max"][0] - meta["max_cut"]) <= 1e-12
+    assert abs(vals["cost4"][0] - 2.4) <= 1e-12 and abs(vals["cost36"][0] - 4.8) <= 1e-12
+    assert abs(vals["expect"][0] - meta["expectation"]) <= 1e-12
+    assert np.max(np.abs(np.asarray(vals["h1"]) - z["w_ring6/hist0"])) <= 1e-12
+    assert np.max(np.abs(np.asarray(vals["h2"]) - z["w_ring6/hist1"])) <= 1e-12
+    o = oracle.OracleRegister(6, "", 0)
+    o.SetStateVector(z["w_ring6/psi"])
+    assert np.max(np.abs(np.asarray(vals["stat"]) - oracle.oracle_google_stats(o)) /
+                  np.maximum(1.0, np.abs(oracle.oracle_google_stats(o)))) <= 1e-12
+    ring = [[1 if abs(i - j) in (1, 5) else 0 for j in range(6)] for i in range(6)]
+    d = oracle.OracleRegister(6, "base", 0)
+    m2 = oracle.oracle_maxcut_cost(d, np.asarray(ring, dtype=np.int32))
+    assert np.max(np.abs(np.asarray(vals["h0"]) - oracle.oracle_cost_histogram(o, d, 0, m2))) <= 1e-12
+    small = iqs.QubitRegister(2, "base", 2)
+    small.ApplyHadamard(0)
+    small.Print("small")
+    assert "\n".join(text) + "\n" == capsys.readouterr().out
