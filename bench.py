@@ -506,6 +506,7 @@ def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int
     t_fwd = time.perf_counter() - t0
     fwd_sweeps = chain.sweeps_forward
     chain.sweeps_forward = 0
+    norm_after = float(chain.psi.ComputeNorm())
     del chain
     gchain = XXZChain(n, J, steps=grad_steps, precision="SP",
                       checkpoint_every=every if (every and grad_steps > every) else None, tile_qubits=tile_qubits)
@@ -519,6 +520,7 @@ def trotter_section(n: int = 32, steps: int = 100, n_dp: int = 33, steps_dp: int
                  "forward_gbs_algorithmic": round(gates * 2 * N * 8 / t_fwd / 1e9, 1),
                  "forward_pass_gbs": round(fwd_sweeps * 2 * N * 8 / t_fwd / 1e9, 1),
                  "zz_first4": [round(float(x), 8) for x in zz[:4]], "zz_mean": float(np.mean(zz)),
+                 "norm_after_forward": norm_after,
                  "gradient": {"strang_steps": grad_steps, "energy": e,
                               "grad_first4": [round(float(x), 8) for x in grad[:4]],
                               "grad_norm": float(np.linalg.norm(grad)),

@@ -137,6 +137,15 @@ class XXZChain:
         self.sweeps_forward += sweeps.value
 
     # ---- forward ----------------------------------------------------------------------------
+    def undo(self, J: Optional[Sequence[float]] = None) -> None:
+        """psi <- circuit(J)^dagger psi: the layers in reverse order with every bond gate
+        inverted (bonds of one layer commute)."""
+        J = self.J if J is None else np.asarray(J, dtype=np.float64)
+        ops = []
+        for bonds, tau in reversed(self.layers()):
+            ops += self._layer_ops((bonds, -tau), J)
+        self._apply(ops)
+
     def forward(self, J: Optional[Sequence[float]] = None, keep_checkpoints: bool = False) -> None:
         """psi <- circuit(J) |Neel>; with keep_checkpoints, store the state at every
         checkpoint boundary."""

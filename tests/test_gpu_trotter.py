@@ -183,3 +183,15 @@ def test_adjoint_ops_reject_bad_input():
     assert lib.iqsg_adjoint_ops(a._h, b._h, bad, 1, gp, 4, None) == _lib.IQSG_EINVAL
     assert lib.iqsg_apply_ops(a._h, good, 1, None) == _lib.IQSG_EINVAL  # gradient ops need two registers
     assert b"iqsg_apply_ops" in lib.iqsg_last_error()
+
+
+@pytest.mark.parametrize("precision,n,tol", [("SP", 26, 1e-4), ("DP", 22, 1e-12)])
+def test_round_trip_returns_to_the_neel_state(precision, n, tol):
+    """Size-independent check: the circuit followed by its inverse is the identity."""
+    from iqs_gb300.trotter import XXZChain
+    J = couplings(n, seed=3)
+    chain = XXZChain(n, J, steps=8, precision=precision, checkpoint_every=None)
+    chain.forward()
+    assert abs(chain.psi.ComputeNorm() - 1.0) <= tol
+    chain.undo()
+    assert abs(abs(chain.psi[chain.neel_index()]) ** 2 - 1.0) <= tol
