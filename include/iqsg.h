@@ -116,6 +116,13 @@ int iqsg_get_amplitude(iqsg_state* h, uint64_t data_index, double* re_im);
 int iqsg_upload(iqsg_state* h, const void* host, uint64_t offset, uint64_t count);
 int iqsg_download(iqsg_state* h, void* host, uint64_t offset, uint64_t count);
 
+/* Uniform random amplitudes: the real and imaginary parts, interleaved in data order, are the
+ * values a + (b - a) u of std::uniform_real_distribution<T>(0, 1) over std::mt19937(seed), T the
+ * register's base type, after discarding the first `skip` values -- the numbers the reference's
+ * RandomNumberGenerator stream with that seed gives (src/rng_utils.cpp:84-160), as used by
+ * Initialize("rand") (src/qureg_init.cpp:253-330; normalise afterwards). Generated on the host. */
+int iqsg_init_uniform_random(iqsg_state* h, uint64_t seed, uint64_t skip, double a, double b);
+
 /* The same copies queued on the register's stream without waiting: they run in order with the
  * register's gates, so a caller can overlap one register's transfers with another register's
  * work. The host memory must stay valid, and unread (upload) or untouched (download), until

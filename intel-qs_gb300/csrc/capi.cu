@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -427,6 +428,33 @@ int iqsg_download(iqsg_state* h, void* host, uint64_t offset, uint64_t count) {
                                    h->stream), "iqsg_download");
   if (st) return st;
   return sync_and_check(h, "iqsg_download");
+}
+
+int iqsg_init_uniform_random(iqsg_state* h, uint64_t seed, uint64_t skip, double a, double b) {
+  int st = check_h(h);
+  if (st) return st;
+  // Host generation in the register's precision with the standard library's std::mt19937 and
+  // std::uniform_real_distribution, staged to HBM in chunks.
+  constexpr uint64_t kChunk = uint64_t(1) << 22;  // amplitudes per copy
+  std::mt19937 gen((std::mt19937::result_type)seed);
+  auto fill = [&](auto r) -> int {
+    using R = decltype(r);
+    std::uniform_real_distribution<R> u((R)0.0, (R)1.0);
+    for (uint64_t k = 0; k < skip; ++k) (void)u(gen);
+    const R ra = (R)a, rb = (R)b;
+    std::vector<R> buf(2 * std::min(kChunk, h->N));
+    for (uint64_t off = 0; off < h->N; off += kChunk) {
+      const uint64_t cnt = std::min(kChunk, h->N - off);
+      for (uint64_t i = 0; i < 2 * cnt; ++i) buf[i] = ra + (rb - ra) * u(gen);
+      int e = cuda_status(cudaMemcpyAsync(static_cast<char*>(h->amps) + off * 2 * sizeof(R), buf.data(),
+                                          2 * cnt * sizeof(R), cudaMemcpyHostToDevice, h->stream),
+                          "iqsg_init_uniform_random");
+      if (!e) e = cuda_status(cudaStreamSynchronize(h->stream), "iqsg_init_uniform_random");
+      if (e) return e;
+    }
+    return IQSG_OK;
+  };
+  return h->prec == IQSG_COMPLEX_DP ? fill((double)0) : fill((float)0);
 }
 
 int iqsg_upload_async(iqsg_state* h, const void* host, uint64_t offset, uint64_t count) {

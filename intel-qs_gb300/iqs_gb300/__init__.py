@@ -13,6 +13,7 @@ from .permutation import GateCounter, Permutation
 from .qureg import QubitRegister
 from .adjoint import QaoaMaxCut, qaoa_energy
 from .batched import BatchedAnsatz
+from .rng import RandomNumberGenerator
 from .trotter import XXZChain
 from .qaoa import (GetExpectationValueFromCostFunction, GetExpectationValueSquaredFromCostFunction,
                    GetHistogramFromCostFunction, GetHistogramFromCostFunctionWithWeightsBinned,
@@ -25,5 +26,5 @@ __all__ = [
     "GetExpectationValueFromCostFunction", "GetExpectationValueSquaredFromCostFunction",
     "InitializeVectorAsWeightedMaxCutCostFunction", "GetHistogramFromCostFunction",
     "GetHistogramFromCostFunctionWithWeightsRounded", "GetHistogramFromCostFunctionWithWeightsBinned",
-    "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz", "XXZChain",
+    "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz", "XXZChain", "RandomNumberGenerator",
 ]

@@ -63,6 +63,7 @@ SIGNATURES = {
     "iqsg_get_amplitude": [_P, _U64, _DP],
     "iqsg_upload": [_P, _P, _U64, _U64],
     "iqsg_download": [_P, _P, _U64, _U64],
+    "iqsg_init_uniform_random": [_P, _U64, _U64, _D, _D],
     "iqsg_upload_async": [_P, _P, _U64, _U64],
     "iqsg_download_async": [_P, _P, _U64, _U64],
     "iqsg_copy": [_P, _P],

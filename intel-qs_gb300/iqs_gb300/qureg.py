@@ -103,6 +103,7 @@ class QubitRegister:
         return self
 
     def _init_flags(self):
+        self._rng = None
         self.gate_counter: Optional[GateCounter] = None
         self._queue = []
         self.fusion = False
@@ -180,10 +181,38 @@ class QubitRegister:
         elif style == "":
             check(lib.iqsg_fill(self._h, 0.0, 0.0))
         elif style == "rand":
-            raise NotImplementedError("Initialize('rand') draws from the reference RNG streams; "
-                                      "upload a seeded state with SetStateVector instead")
+            # src/qureg_init.cpp:253-330: real and imaginary parts uniform in [-1, 1) from the
+            # register's RNG ("pool" stream for base_index 0, "local" for base_index = number of
+            # states = 1), the stream advanced by 2 * 2^n, then the state normalised.
+            rng = self._rng
+            if rng is None:
+                raise ValueError("Initialize('rand'): set a RandomNumberGenerator with SetRngPtr first")
+            if rng.GetSeed() == 0:
+                raise ValueError("Initialize('rand'): the RandomNumberGenerator needs a nonzero seed")
+            if base_index not in (0, 1):
+                raise ValueError("Initialize('rand'): base_index must be 0 (pool stream) or 1 (local stream)")
+            shared = "pool" if base_index == 0 else "local"
+            skip = rng._count[shared]
+            check(lib.iqsg_init_uniform_random(self._h, rng.stream_seed(shared), skip, -1.0, 1.0))
+            rng.SkipAhead(2 * self.GlobalSize(), shared)
+            self.Normalize()
         else:
             raise ValueError(f"unknown initialisation style {style!r}")
+
+    # ---- random number generator (include/qureg.hpp:375-379) ----------------------------
+    def SetRngPtr(self, rng) -> None:
+        self._rng = rng
+
+    def GetRngPtr(self):
+        return self._rng
+
+    def ResetRngPtr(self) -> None:
+        self._rng = None
+
+    def SetSeedRngPtr(self, seed: int) -> None:
+        if self._rng is None:
+            raise ValueError("SetSeedRngPtr: no RandomNumberGenerator set")
+        self._rng.SetSeedStreamPtrs(seed)
 
     def InitializationWithSameAmplitudeEverywhere(self, amplitude: complex) -> None:
         a = complex(amplitude)

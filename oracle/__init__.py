@@ -431,6 +431,26 @@ def oracle_cost_histogram(psi: OracleRegister, diag: OracleRegister, mode: int, 
     return np.bincount(b, weights=p, minlength=nb)[:nb]
 
 
+def oracle_uniform_random(seed: int, skip: int, count: int, a: float, b: float, precision: str = "DP") -> np.ndarray:
+    """The numbers of the reference's RandomNumberGenerator stream (src/rng_utils.cpp:84-160):
+    std::mt19937 seeded with seed (the 32-bit init_genrand seeding, as numpy's legacy seeding),
+    std::uniform_real_distribution over it as the C++ standard library computes it -- for
+    double two 32-bit draws, u = (g1 + g2 2^32) / 2^64 in double; for float one draw,
+    u = float(g1) / 2^32 -- then a + (b - a) u in the same type; the first `skip` values are
+    dropped."""
+    bg = np.random.MT19937()
+    bg._legacy_seeding(int(seed) & 0xFFFFFFFF)
+    if precision == "DP":
+        raw = bg.random_raw(2 * (skip + count)).astype(np.float64).reshape(-1, 2)
+        u = (raw[:, 0] + raw[:, 1] * 4294967296.0) / 18446744073709551616.0
+        u = np.where(u >= 1.0, np.nextafter(1.0, 0.0), u)[skip:]
+        return a + (b - a) * u
+    raw = bg.random_raw(skip + count).astype(np.float32)
+    u = raw / np.float32(4294967296.0)
+    u = np.where(u >= np.float32(1.0), np.nextafter(np.float32(1.0), np.float32(0.0)), u)[skip:]
+    return np.float32(a) + (np.float32(b) - np.float32(a)) * u
+
+
 def oracle_google_stats(reg: OracleRegister) -> list:
     """GoogleStats (src/qureg_utils.cpp:349-450) restated with numpy: entropy, average
     self-information and the scaled moments m2..m10 of p = |amp|^2."""
@@ -476,6 +496,7 @@ def rlib() -> C.CDLL:
             "ref_qaoa_expectation": ([_P, _P], _D), "ref_qaoa_expectation_sq": ([_P, _P], _D),
             "ref_qaoa_weighted_cost": ([_P, _DP, _U], _D),
             "ref_entropy": ([_P], _D), "ref_google_stats": ([_P, _DP, C.c_int], C.c_int),
+            "ref_init_rand": ([_P, C.c_ulong, C.c_int, C.c_int], None),
             "ref_print": ([_P, C.c_char_p], None), "ref_export": ([_P, C.c_char_p], None),
             "ref_qaoa_histogram": ([_P, _P, C.c_int, _D, _D, _DP, C.c_int], C.c_int),
         }

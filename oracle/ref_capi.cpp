@@ -185,6 +185,17 @@ int ref_qaoa_histogram(RefReg* psi, RefReg* diag, int mode, double max_value, do
   });
   return len;
 }
+// Initialize("rand", base_index) `times` times in a row with a RandomNumberGenerator seeded with seed.
+void ref_init_rand(RefReg* h, unsigned long seed, int base_index, int times) {
+  DISPATCH(h, {
+    auto* rng = new iqs::RandomNumberGenerator<typename QubitRegister<T>::BaseType>();
+    rng->SetSeedStreamPtrs(seed);
+    q->SetRngPtr(rng);
+    for (int t = 0; t < times; ++t) q->Initialize("rand", (std::size_t)base_index);
+    q->ResetRngPtr();
+    delete rng;
+  });
+}
 double ref_entropy(RefReg* h) {
   double r = 0;
   DISPATCH(h, r = q->Entropy());

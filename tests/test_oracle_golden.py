@@ -122,3 +122,20 @@ def test_oracle_google_stats_golden():
         got = np.asarray(oracle.oracle_google_stats(r))
         tol = 1e-12 if meta["precision"] == "DP" else 1e-5
         assert np.max(np.abs(got - want) / np.maximum(1.0, np.abs(want))) <= tol, name
+
+
+def test_oracle_random_init_golden():
+    """Initialize("rand") restated (numpy MT19937 with the C++ standard library's uniform
+    distribution) against the reference's own states."""
+    import json
+    z = np.load(REPO / "tests" / "golden" / "rand_init.npz")
+    for name in sorted({k.split("/")[0] for k in z.files}):
+        meta = json.loads(str(z[f"{name}/meta"]))
+        n, prec, seed = meta["n"], meta["precision"], meta["seed"]
+        stream_seed = seed if meta["base_index"] == 0 else seed + 2  # "pool" or "local" stream
+        skip = 2 * (1 << n) * (meta["times"] - 1)
+        v = oracle.oracle_uniform_random(stream_seed, skip, 2 * (1 << n), -1.0, 1.0, prec).astype(np.float64)
+        st = v[0::2] + 1j * v[1::2]
+        st /= np.linalg.norm(st)
+        tol = 1e-14 if prec == "DP" else 1e-6
+        assert np.max(np.abs(st - z[f"{name}/state"])) <= tol, name
