@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "../iqsg.h"
+#include "noise.hpp"
 
 using ComplexSP = std::complex<float>;
 using ComplexDP = std::complex<double>;
@@ -220,10 +221,61 @@ class QubitRegister {
       check_status(iqsg_fill(h_, (BaseType)(1. / std::sqrt((double)GlobalSize())), 0.0));
     } else if (style.empty()) {
       check_status(iqsg_fill(h_, 0.0, 0.0));
+    } else if (style == "rand") {
+      // src/qureg_init.cpp:256-333: uniform real and imaginary parts in [-1, 1) from the "pool"
+      // stream (base_index 0) or the "local" one (base_index = number of states = 1), normalised.
+      if (!rng_ptr_) throw std::invalid_argument("Initialize(\"rand\"): SetRngPtr first");
+      if (base_index > 1) throw std::invalid_argument("Initialize(\"rand\"): base_index must be 0 or 1");
+      check_status(iqsg_init_random(h_, rng_ptr_->handle(), base_index == 0 ? 0 : 2));
+      Normalize();
     } else {
-      throw std::invalid_argument("Initialize: style must be \"base\", \"++++\" or \"\"");
+      throw std::invalid_argument("Initialize: style must be \"base\", \"++++\", \"rand\" or \"\"");
     }
   }
+
+  // ---- random number generator (include/qureg.hpp:375-379) ----
+  RandomNumberGenerator<BaseType>* GetRngPtr() { return rng_ptr_; }
+  void ResetRngPtr() { rng_ptr_ = nullptr; }
+  void SetRngPtr(RandomNumberGenerator<BaseType>* rng_ptr) { rng_ptr_ = rng_ptr; }
+  void SetSeedRngPtr(std::size_t seed) {
+    if (!rng_ptr_) throw std::invalid_argument("SetSeedRngPtr: no RandomNumberGenerator set");
+    rng_ptr_->SetSeedStreamPtrs(seed);
+  }
+
+  // ---- noise (src/qureg_noisysimul.cpp, src/qureg_apply_channel.cpp) ----
+  BaseType GetT1() { return T_1_; }
+  BaseType GetT2() { return T_2_; }
+  BaseType GetTphi() { return T_phi_; }
+  void SetNoiseTimescales(BaseType T1, BaseType T2) {
+    if (!(T2 >= T1 / 2.)) throw std::invalid_argument("SetNoiseTimescales: T2 must be at least T1/2");
+    T_1_ = T1;
+    T_2_ = T2;
+    T_phi_ = 1. / (1. / T2 - 1. / (2. * T1));
+  }
+  // Pauli-twirl noise for `duration` (three Gaussian angles from the "state" stream, one gate).
+  void ApplyNoiseGate(const unsigned qubit, const BaseType duration) {
+    if (!rng_ptr_) throw std::invalid_argument("ApplyNoiseGate: SetRngPtr first");
+    if (duration == 0) return;
+    double m[8];
+    check_status(iqsg_noise_gate_draw(rng_ptr_->handle(), kPrec, T_1_, T_2_, duration, m));
+    QubitRegister::Apply1QubitGate(qubit, mat2(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7]));
+  }
+  // One eigenvector of chi, drawn from the "state" stream, applied as a gate; a negative
+  // eigenvalue flips the overall sign.
+  void ApplyChannel(const unsigned qubit, CM4x4<Type>& chi) {
+    double g[8];
+    channel_draw(4, chi, g);
+    QubitRegister::Apply1QubitGate(qubit, mat2(g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7]));
+  }
+  void ApplyChannel(const unsigned qubit1, const unsigned qubit2, CM16x16<Type>& chi) {
+    double g[32];
+    channel_draw(16, chi, g);
+    TM4x4<Type> m;
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) m(r, c) = Type((BaseType)g[2 * (4 * r + c)], (BaseType)g[2 * (4 * r + c) + 1]);
+    QubitRegister::Apply2QubitGate(qubit1, qubit2, m);
+  }
+  BaseType GetOverallSignOfChannels() { return overall_sign_of_channels; }
   void InitializationWithSameAmplitudeEverywhere(Type a) {
     ApplyFusedGates();
     check_status(iqsg_fill(h_, a.real(), a.imag()));
@@ -613,6 +665,21 @@ class QubitRegister {
     other.ApplyFusedGates();
   }
 
+  template <class Chi>
+  void channel_draw(unsigned M, const Chi& chi, double* gate) {
+    if (!rng_ptr_) throw std::invalid_argument("ApplyChannel: SetRngPtr first");
+    std::vector<double> ev, cum, vecs;
+    chi.channel_arrays(ev, cum, vecs);
+    unsigned k = 0;
+    int negative = 0;
+    check_status(iqsg_channel_gate(rng_ptr_->handle(), kPrec, M, ev.data(), cum.data(), vecs.data(), gate, &k,
+                                   &negative));
+    if (negative) overall_sign_of_channels *= -1;
+  }
+
+  RandomNumberGenerator<BaseType>* rng_ptr_ = nullptr;
+  BaseType T_1_ = 0, T_2_ = 0, T_phi_ = 0;
+  BaseType overall_sign_of_channels = 1;
   unsigned n_;
   iqsg_state* h_ = nullptr;
   Permutation perm_;
@@ -623,3 +690,11 @@ class QubitRegister {
 };
 
 }  // namespace iqs
+
+// The reference declares the matrix aliases at global scope (include/qureg.hpp:44-55).
+template <class Type>
+using TM2x2 = iqs::TinyMatrix<Type, 2, 2, 32>;
+template <class Type>
+using TM4x4 = iqs::TinyMatrix<Type, 4, 4, 32>;
+
+#include "noisy_qureg.hpp"

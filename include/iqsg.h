@@ -123,6 +123,62 @@ int iqsg_download(iqsg_state* h, void* host, uint64_t offset, uint64_t count);
  * Initialize("rand") (src/qureg_init.cpp:253-330; normalise afterwards). Generated on the host. */
 int iqsg_init_uniform_random(iqsg_state* h, uint64_t seed, uint64_t skip, double a, double b);
 
+/* ---- random numbers, noise gates, chi-matrix channels (host side; the gates they produce go
+ * through iqsg_apply_1q / iqsg_apply_2q) ---- */
+
+/* Random number streams with the structure of the reference's RandomNumberGenerator
+ * (include/rng_utils.hpp:46-130, src/rng_utils.cpp:13-225): three std::mt19937 streams,
+ * 0 "pool" (seed), 1 "state" (seed + 1) and 2 "local" (seed + 2) -- one process being one state
+ * of a one-state pool -- sharing one std::uniform_real_distribution and one
+ * std::normal_distribution per base type, with per-stream counts: a uniform counts 1, a Gaussian
+ * 2, a skip draws and discards uniforms. `precision` (IQSG_COMPLEX_SP / _DP) picks the base type
+ * (float / double) as the reference's template argument does; values are returned as doubles. */
+typedef struct iqsg_rng iqsg_rng;
+int iqsg_rng_create(iqsg_rng** out);
+void iqsg_rng_destroy(iqsg_rng* r);
+/* Copy constructor (src/rng_utils.cpp:13-20): same seed, each stream's count skipped. */
+int iqsg_rng_clone(const iqsg_rng* src, int precision, iqsg_rng** out);
+int iqsg_rng_set_seed(iqsg_rng* r, uint64_t seed);                          /* SetSeedStreamPtrs */
+int iqsg_rng_skip(iqsg_rng* r, int precision, uint64_t n, int stream);       /* SkipAhead */
+int iqsg_rng_uniform(iqsg_rng* r, int precision, double* out, uint64_t n, double a, double b,
+                     int stream);                                            /* UniformRandomNumbers */
+int iqsg_rng_gaussian(iqsg_rng* r, int precision, double* out, uint64_t n, int stream);
+int iqsg_rng_integers(iqsg_rng* r, int precision, int* out, uint64_t n, int a, int b,
+                      int stream);                                           /* RandomIntegersInRange */
+int iqsg_rng_info(const iqsg_rng* r, uint64_t* seed, uint64_t* counts /* [3] */);
+/* Initialize("rand") (src/qureg_init.cpp:256-333) without its final normalisation: amplitudes
+ * uniform in [-1, 1) from a copy of r on the stream (0 pool, 2 local), then r skips 2 * 2^n. */
+int iqsg_init_random(iqsg_state* h, iqsg_rng* r, int stream);
+
+/* The Pauli-twirl noise gate of ApplyNoiseGate (src/qureg_noisysimul.cpp:33-85) as a 2x2
+ * row-major complex matrix, from three standard Gaussians `gauss`, computed in the base type. */
+int iqsg_noise_gate_matrix(int precision, double T1, double T2, double duration, const double* gauss,
+                           double* m8);
+/* The same with the three Gaussians drawn from r's "state" stream, as ApplyNoiseGate draws them. */
+int iqsg_noise_gate_draw(iqsg_rng* r, int precision, double T1, double T2, double duration, double* m8);
+/* NoisyQureg's own Gaussian source (include/NoisyQureg.hpp:47-66): std::default_random_engine
+ * seeded with `seed` and a std::normal_distribution of the base type. */
+typedef struct iqsg_noise_engine iqsg_noise_engine;
+int iqsg_noise_engine_create(uint32_t seed, iqsg_noise_engine** out);
+void iqsg_noise_engine_destroy(iqsg_noise_engine* e);
+int iqsg_noise_engine_gaussian(iqsg_noise_engine* e, int precision, double* out, uint64_t n);
+
+/* Chi matrices (include/chi_matrix.hpp, src/chi_matrix.cpp): M x M complex, row-major
+ * interleaved. iqsg_chi_eigensystem replaces SolveEigenSystem: eigenvalues (2M doubles),
+ * standardised eigenvectors (row k = eigenvector k, 2M*M doubles), probabilities |E_k|/sum|E| and
+ * their running sums; eigenvectors scaled by sqrt(sum |E|). chi must be Hermitian. Order:
+ * increasing |E_k|; phase: largest component real and positive. iqsg_chi_normalize is the
+ * reference's NormalizeEigenProbAndRenormalizeEigenVect for an eigensystem given by the caller. */
+int iqsg_chi_eigensystem(int precision, unsigned M, const double* chi, double* evals, double* evecs,
+                         double* probs, double* cumprobs);
+int iqsg_chi_normalize(int precision, unsigned M, const double* evals, double* evecs, double* probs,
+                       double* cumprobs);
+/* One draw of ApplyChannel (src/qureg_apply_channel.cpp:17-106): a uniform on r's "state" stream
+ * selects eigenvector k; `gate` receives the 2x2 (M = 4) or 4x4 (M = 16) matrix to apply with
+ * iqsg_apply_1q / iqsg_apply_2q; *negative = 1 when E_k < 0 (the register's overall sign flips). */
+int iqsg_channel_gate(iqsg_rng* r, int precision, unsigned M, const double* evals, const double* cumprobs,
+                      const double* evecs, double* gate, unsigned* k_out, int* negative);
+
 /* The same copies queued on the register's stream without waiting: they run in order with the
  * register's gates, so a caller can overlap one register's transfers with another register's
  * work. The host memory must stay valid, and unread (upload) or untouched (download), until

@@ -14,6 +14,8 @@ from .qureg import QubitRegister
 from .adjoint import QaoaMaxCut, qaoa_energy
 from .batched import BatchedAnsatz
 from .rng import RandomNumberGenerator
+from .chi import CM4x4, CM16x16, ChiMatrix
+from .noisy import NoisyQureg
 from .trotter import XXZChain
 from .qaoa import (GetExpectationValueFromCostFunction, GetExpectationValueSquaredFromCostFunction,
                    GetHistogramFromCostFunction, GetHistogramFromCostFunctionWithWeightsBinned,
@@ -26,5 +28,5 @@ __all__ = [
     "GetExpectationValueFromCostFunction", "GetExpectationValueSquaredFromCostFunction",
     "InitializeVectorAsWeightedMaxCutCostFunction", "GetHistogramFromCostFunction",
     "GetHistogramFromCostFunctionWithWeightsRounded", "GetHistogramFromCostFunctionWithWeightsBinned",
-    "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz", "XXZChain", "RandomNumberGenerator",
+    "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz", "XXZChain", "RandomNumberGenerator", "ChiMatrix", "CM4x4", "CM16x16", "NoisyQureg",
 ]

@@ -64,6 +64,24 @@ SIGNATURES = {
     "iqsg_upload": [_P, _P, _U64, _U64],
     "iqsg_download": [_P, _P, _U64, _U64],
     "iqsg_init_uniform_random": [_P, _U64, _U64, _D, _D],
+    "iqsg_rng_create": [C.POINTER(_P)],
+    "iqsg_rng_destroy": [_P],
+    "iqsg_rng_clone": [_P, C.c_int, C.POINTER(_P)],
+    "iqsg_rng_set_seed": [_P, _U64],
+    "iqsg_rng_skip": [_P, C.c_int, _U64, C.c_int],
+    "iqsg_rng_uniform": [_P, C.c_int, _DP, _U64, _D, _D, C.c_int],
+    "iqsg_rng_gaussian": [_P, C.c_int, _DP, _U64, C.c_int],
+    "iqsg_rng_integers": [_P, C.c_int, C.POINTER(C.c_int), _U64, C.c_int, C.c_int, C.c_int],
+    "iqsg_rng_info": [_P, C.POINTER(_U64), C.POINTER(_U64)],
+    "iqsg_init_random": [_P, _P, C.c_int],
+    "iqsg_noise_gate_matrix": [C.c_int, _D, _D, _D, _DP, _DP],
+    "iqsg_noise_gate_draw": [_P, C.c_int, _D, _D, _D, _DP],
+    "iqsg_noise_engine_create": [C.c_uint32, C.POINTER(_P)],
+    "iqsg_noise_engine_destroy": [_P],
+    "iqsg_noise_engine_gaussian": [_P, C.c_int, _DP, _U64],
+    "iqsg_chi_eigensystem": [C.c_int, C.c_uint, _DP, _DP, _DP, _DP, _DP],
+    "iqsg_chi_normalize": [C.c_int, C.c_uint, _DP, _DP, _DP, _DP],
+    "iqsg_channel_gate": [_P, C.c_int, C.c_uint, _DP, _DP, _DP, _DP, C.POINTER(C.c_uint), C.POINTER(C.c_int)],
     "iqsg_upload_async": [_P, _P, _U64, _U64],
     "iqsg_download_async": [_P, _P, _U64, _U64],
     "iqsg_copy": [_P, _P],
@@ -105,7 +123,7 @@ SIGNATURES = {
     "iqsg_batch_info": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
     "iqsg_probability_static": [_P, _U, C.c_int, _U, _P, _P],
 }
-_RESTYPES = {"iqsg_last_error": C.c_char_p}
+_RESTYPES = {"iqsg_last_error": C.c_char_p, "iqsg_rng_destroy": None, "iqsg_noise_engine_destroy": None}
 
 
 def _load() -> C.CDLL:

@@ -171,7 +171,7 @@ class QubitRegister:
 
     # ---- state initialisation / access -----------------------------------------------
     def Initialize(self, style: str = "", base_index: int = 0) -> None:
-        """src/qureg_init.cpp:225-359 ("rand" needs the reference RNG and is not offered)."""
+        """src/qureg_init.cpp:225-359: "base", "++++", "" (all zero) and "rand" (needs SetRngPtr)."""
         if style == "base":
             if not 0 <= base_index < self.GlobalSize():
                 raise ValueError(f"base_index {base_index} out of range")
@@ -191,10 +191,8 @@ class QubitRegister:
                 raise ValueError("Initialize('rand'): the RandomNumberGenerator needs a nonzero seed")
             if base_index not in (0, 1):
                 raise ValueError("Initialize('rand'): base_index must be 0 (pool stream) or 1 (local stream)")
-            shared = "pool" if base_index == 0 else "local"
-            skip = rng._count[shared]
-            check(lib.iqsg_init_uniform_random(self._h, rng.stream_seed(shared), skip, -1.0, 1.0))
-            rng.SkipAhead(2 * self.GlobalSize(), shared)
+            self._flush()
+            check(lib.iqsg_init_random(self._h, rng.handle, 0 if base_index == 0 else 2))
             self.Normalize()
         else:
             raise ValueError(f"unknown initialisation style {style!r}")
@@ -213,6 +211,74 @@ class QubitRegister:
         if self._rng is None:
             raise ValueError("SetSeedRngPtr: no RandomNumberGenerator set")
         self._rng.SetSeedStreamPtrs(seed)
+
+    # ---- noise (src/qureg_noisysimul.cpp, src/qureg_apply_channel.cpp) --------------------
+    def SetNoiseTimescales(self, T1: float, T2: float) -> None:
+        """Dissipation time T1 and decoherence time T2 (T2 >= T1/2); T_phi = 1/(1/T2 - 1/(2 T1))."""
+        T1, T2 = self._bt(T1), self._bt(T2)
+        if not T2 >= T1 / 2.0:
+            raise ValueError(f"SetNoiseTimescales: T2 = {T2} must be at least T1/2 = {T1 / 2.0}")
+        self._T1, self._T2 = T1, T2
+        with np.errstate(divide="ignore"):
+            self._Tphi = self._bt(1.0 / (1.0 / T2 - 1.0 / (2.0 * T1))) if T2 != T1 / 2.0 else float("inf")
+
+    def GetT1(self) -> float:
+        return getattr(self, "_T1", 0.0)
+
+    def GetT2(self) -> float:
+        return getattr(self, "_T2", 0.0)
+
+    def GetTphi(self) -> float:
+        return getattr(self, "_Tphi", 0.0)
+
+    def ApplyNoiseGate(self, qubit: int, duration: float) -> None:
+        """Pauli-twirl noise for `duration` on `qubit` (src/qureg_noisysimul.cpp:33-85): three
+        Gaussian angles from the RNG's "state" stream, one 1-qubit gate."""
+        if self._rng is None:
+            raise ValueError("ApplyNoiseGate: set a RandomNumberGenerator with SetRngPtr first")
+        if not hasattr(self, "_T1"):
+            raise ValueError("ApplyNoiseGate: call SetNoiseTimescales first")
+        duration = self._bt(duration)
+        if duration == 0:
+            return
+        m = np.zeros(8)
+        check(lib.iqsg_noise_gate_draw(self._rng.handle, self._prec, self._T1, self._T2, duration,
+                                       m.ctypes.data_as(_lib._DP)))
+        QubitRegister.Apply1QubitGate(self, qubit, m.view(np.complex128).reshape(2, 2))
+
+    def ApplyChannel(self, *args) -> None:
+        """ApplyChannel(qubit, chi) with a 4x4 chi matrix, or ApplyChannel(qubit1, qubit2, chi)
+        with a 16x16 one (src/qureg_apply_channel.cpp:17-106): one eigenvector of chi, drawn with
+        probability |E_k| / sum |E| from the RNG's "state" stream, applied as a gate; a negative
+        eigenvalue flips GetOverallSignOfChannels()."""
+        if len(args) == 2:
+            qubits, chi, M = args[:1], args[1], 4
+        elif len(args) == 3:
+            qubits, chi, M = args[:2], args[2], 16
+        else:
+            raise TypeError("ApplyChannel(qubit, chi) or ApplyChannel(qubit1, qubit2, chi)")
+        if getattr(chi, "M", None) != M:
+            raise ValueError(f"ApplyChannel on {len(qubits)} qubit(s) needs a {M}x{M} chi matrix")
+        if chi.precision != self.precision:
+            raise ValueError(f"ApplyChannel: chi matrix is {chi.precision}, the register {self.precision}")
+        if self._rng is None:
+            raise ValueError("ApplyChannel: set a RandomNumberGenerator with SetRngPtr first")
+        ev, cum, vf = chi._arrays()
+        gate = np.zeros(2 * (2 if M == 4 else 4) ** 2)
+        k, neg = C.c_uint(), C.c_int()
+        check(lib.iqsg_channel_gate(self._rng.handle, self._prec, M, ev.ctypes.data_as(_lib._DP),
+                                    cum.ctypes.data_as(_lib._DP), vf.ctypes.data_as(_lib._DP),
+                                    gate.ctypes.data_as(_lib._DP), C.byref(k), C.byref(neg)))
+        if neg.value:
+            self._overall_sign = -self.GetOverallSignOfChannels()
+        g = gate.view(np.complex128)
+        if M == 4:
+            QubitRegister.Apply1QubitGate(self, qubits[0], g.reshape(2, 2))
+        else:
+            QubitRegister.Apply2QubitGate(self, qubits[0], qubits[1], g.reshape(4, 4))
+
+    def GetOverallSignOfChannels(self) -> float:
+        return getattr(self, "_overall_sign", 1.0)
 
     def InitializationWithSameAmplitudeEverywhere(self, amplitude: complex) -> None:
         a = complex(amplitude)

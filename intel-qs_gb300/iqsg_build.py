@@ -24,7 +24,7 @@ QASM_SRC = ROOT / "qasm" / "iqsg_qasm.cpp"
 QASM = PKG_DIR / "iqsg_qasm"                 # QASM front end over the C++ drop-in header
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
 
 

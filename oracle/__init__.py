@@ -499,6 +499,12 @@ def rlib() -> C.CDLL:
             "ref_init_rand": ([_P, C.c_ulong, C.c_int, C.c_int], None),
             "ref_print": ([_P, C.c_char_p], None), "ref_export": ([_P, C.c_char_p], None),
             "ref_qaoa_histogram": ([_P, _P, C.c_int, _D, _D, _DP, C.c_int], C.c_int),
+            "ref_rng_sequence": ([C.c_int, C.c_ulong, _IP, C.c_int, _DP, C.c_int, C.POINTER(C.c_ulong)], C.c_int),
+            "ref_noise_run": ([_P, C.c_ulong, _D, _D, _UP, _DP, C.c_int, C.POINTER(C.c_ulong)], None),
+            "ref_noisy_qureg_run": ([C.c_int, _U, _U, _D, _D, _D, _D, _IP, _DP, _DP, C.c_int, _DP, _UP], None),
+            "ref_chi_normalize": ([C.c_int, _U, _DP, _DP, _DP, _DP, _DP], None),
+            "ref_channel_run": ([_P, C.c_ulong, _U, _DP, _DP, _UP, C.c_int], _D),
+            "ref_ideal_hadamard_channel": ([_P, C.c_ulong, _U, C.c_int], None),
         }
         for name, (args, res) in sigs.items():
             fn = getattr(L, name)

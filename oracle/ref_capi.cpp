@@ -221,4 +221,190 @@ double ref_qaoa_expectation_sq(RefReg* psi, RefReg* diag) {
   return r;
 }
 
+
 }  // extern "C"
+
+// ---- random numbers, noise gates, channels ----
+
+// A sequence of draws on one RandomNumberGenerator<float|double>: ops holds triples
+// (kind, n, stream) -- kind 0 uniform [0,1), 1 uniform [-2,5), 2 Gaussian, 3 integers in [-3,17),
+// 4 SkipAhead, 5 replace the generator by a copy of itself (copy constructor); stream 0 pool,
+// 1 state, 2 local. Values drawn are appended to out; counts[3] receives the final counts.
+template <class B>
+static int rng_sequence(unsigned long seed, const int* ops, int nops, double* out, int cap, unsigned long* counts) {
+  static const char* names[3] = {"pool", "state", "local"};
+  auto* rng = new iqs::RandomNumberGenerator<B>();
+  rng->SetSeedStreamPtrs(seed);
+  int len = 0;
+  for (int i = 0; i < nops; ++i) {
+    const int kind = ops[3 * i], n = ops[3 * i + 1];
+    const std::string st = names[ops[3 * i + 2]];
+    std::vector<B> v(n > 0 ? n : 1);
+    std::vector<int> iv(n > 0 ? n : 1);
+    if (kind == 0) rng->UniformRandomNumbers(v.data(), n, B(0), B(1), st);
+    if (kind == 1) rng->UniformRandomNumbers(v.data(), n, B(-2), B(5), st);
+    if (kind == 2) rng->GaussianRandomNumbers(v.data(), n, st);
+    if (kind == 3) {
+      rng->RandomIntegersInRange(iv.data(), n, -3, 17, st);
+      for (int j = 0; j < n; ++j) v[j] = (B)iv[j];
+    }
+    if (kind == 4) rng->SkipAhead(n, st);
+    if (kind == 5) {
+      auto* c = new iqs::RandomNumberGenerator<B>(rng);
+      delete rng;
+      rng = c;
+    }
+    if (kind <= 3)
+      for (int j = 0; j < n && len < cap; ++j) out[len++] = (double)v[j];
+  }
+  counts[0] = rng->GetNumGeneratedOrSkippedPoolNumbers();
+  counts[1] = rng->GetNumGeneratedOrSkippedStateNumbers();
+  counts[2] = rng->GetNumGeneratedOrSkippedLocalNumbers();
+  delete rng;
+  return len;
+}
+extern "C" int ref_rng_sequence(int sp, unsigned long seed, const int* ops, int nops, double* out, int cap, unsigned long* counts) {
+  return sp ? rng_sequence<float>(seed, ops, nops, out, cap, counts)
+            : rng_sequence<double>(seed, ops, nops, out, cap, counts);
+}
+
+// SetNoiseTimescales(T1, T2), then ApplyNoiseGate(qubits[i], durations[i]) for i < steps with a
+// generator seeded with seed; counts[3] receives the generator's final counts.
+extern "C" void ref_noise_run(RefReg* h, unsigned long seed, double T1, double T2, const unsigned* qubits,
+                   const double* durations, int steps, unsigned long* counts) {
+  DISPATCH(h, {
+    using B = typename QubitRegister<T>::BaseType;
+    iqs::RandomNumberGenerator<B> rng;
+    rng.SetSeedStreamPtrs(seed);
+    q->SetRngPtr(&rng);
+    q->SetNoiseTimescales((B)T1, (B)T2);
+    for (int i = 0; i < steps; ++i) q->ApplyNoiseGate(qubits[i], (B)durations[i]);
+    q->ResetRngPtr();
+    counts[0] = rng.GetNumGeneratedOrSkippedPoolNumbers();
+    counts[1] = rng.GetNumGeneratedOrSkippedStateNumbers();
+    counts[2] = rng.GetNumGeneratedOrSkippedLocalNumbers();
+  });
+}
+
+// A NoisyQureg<Type>(n, seed, T1, T2) program: Initialize("base", 0), SetGateDurations(Ts, Td),
+// then prog triples (kind, a, b) -- 0 H a, 1 RX a, 2 RY a, 3 RZ a (angle angles[i]),
+// 4 CPauliX a b, 5 ApplyControlled1QubitGate a b mats[i], 6 Apply1QubitGate a mats[i],
+// 7 ApplyNoiseGatesOnAllQubits. Writes the state, the 1- and 2-qubit gate counts and the n x n
+// gate-count matrix.
+template <class T>
+static void noisy_run(unsigned n, unsigned seed, double T1, double T2, double Ts, double Td, const int* prog,
+                      const double* angles, const double* mats, int nprog, double* state, unsigned* counts) {
+  using B = typename QubitRegister<T>::BaseType;
+  iqs::NoisyQureg<T> r(n, seed, (B)T1, (B)T2);
+  r.Initialize("base", 0);
+  r.SetGateDurations((B)Ts, (B)Td);
+  for (int i = 0; i < nprog; ++i) {
+    const int kind = prog[3 * i];
+    const unsigned a = (unsigned)prog[3 * i + 1], b = (unsigned)prog[3 * i + 2];
+    if (kind == 0) r.ApplyHadamard(a);
+    if (kind == 1) r.ApplyRotationX(a, (B)angles[i]);
+    if (kind == 2) r.ApplyRotationY(a, (B)angles[i]);
+    if (kind == 3) r.ApplyRotationZ(a, (B)angles[i]);
+    if (kind == 4) r.ApplyCPauliX(a, b);
+    if (kind == 5) r.ApplyControlled1QubitGate(a, b, tm2<T>(mats + 8 * i));
+    if (kind == 6) r.Apply1QubitGate(a, tm2<T>(mats + 8 * i));
+    if (kind == 7) r.ApplyNoiseGatesOnAllQubits();
+  }
+  for (std::size_t i = 0; i < (std::size_t(1) << n); ++i) {
+    const T v = r.GetGlobalAmplitude(i);
+    state[2 * i] = v.real();
+    state[2 * i + 1] = v.imag();
+  }
+  counts[0] = r.GetOneQubitExperimentalGateCount();
+  counts[1] = r.GetTwoQubitExperimentalGateCount();
+  for (unsigned x = 0; x < n; ++x)
+    for (unsigned y = 0; y < n; ++y) counts[2 + x * n + y] = r.GetExperimentalGateCount(x, y);
+}
+extern "C" void ref_noisy_qureg_run(int sp, unsigned n, unsigned seed, double T1, double T2, double Ts, double Td,
+                         const int* prog, const double* angles, const double* mats, int nprog, double* state,
+                         unsigned* counts) {
+  if (sp) noisy_run<CSP>(n, seed, T1, T2, Ts, Td, prog, angles, mats, nprog, state, counts);
+  else noisy_run<CDP>(n, seed, T1, T2, Ts, Td, prog, angles, mats, nprog, state, counts);
+}
+
+// A chi matrix whose eigensystem is given by the caller (the reference's members are protected
+// and its SolveEigenSystem needs Eigen, which is not vendored): eigenvalues, eigenvectors, then
+// the reference's own NormalizeEigenProbAndRenormalizeEigenVect.
+template <class T, unsigned M>
+struct GivenChi : iqs::ChiMatrix<T, M, 32> {
+  GivenChi(const double* evals, const double* evecs) {
+    this->evalues_.assign(M, T(0));
+    this->evectors_.assign(M, std::vector<T>(M, T(0)));
+    for (unsigned k = 0; k < M; ++k) {
+      this->evalues_[k] = T(evals[2 * k], evals[2 * k + 1]);
+      for (unsigned i = 0; i < M; ++i)
+        this->evectors_[k][i] = T(evecs[2 * (k * M + i)], evecs[2 * (k * M + i) + 1]);
+    }
+    this->NormalizeEigenProbAndRenormalizeEigenVect();
+  }
+};
+
+// The normalised eigensystem (probabilities, cumulative probabilities, eigenvectors) of GivenChi.
+template <class T, unsigned M>
+static void chi_normalize(const double* evals, const double* evecs, double* probs, double* cum, double* vecs) {
+  GivenChi<T, M> chi(evals, evecs);
+  for (unsigned k = 0; k < M; ++k) {
+    probs[k] = chi.GetEigenProbability(k);
+    cum[k] = chi.GetEigenCumulativeProbability(k);
+    const std::vector<T> v = chi.GetEigenVector(k);
+    for (unsigned i = 0; i < M; ++i) {
+      vecs[2 * (k * M + i)] = v[i].real();
+      vecs[2 * (k * M + i) + 1] = v[i].imag();
+    }
+  }
+}
+extern "C" void ref_chi_normalize(int sp, unsigned M, const double* evals, const double* evecs, double* probs, double* cum,
+                       double* vecs) {
+  if (M == 4) {
+    if (sp) chi_normalize<CSP, 4>(evals, evecs, probs, cum, vecs);
+    else chi_normalize<CDP, 4>(evals, evecs, probs, cum, vecs);
+  } else {
+    if (sp) chi_normalize<CSP, 16>(evals, evecs, probs, cum, vecs);
+    else chi_normalize<CDP, 16>(evals, evecs, probs, cum, vecs);
+  }
+}
+
+// ApplyChannel `steps` times (qubits: one per step for M = 4, two for M = 16) with a generator
+// seeded with seed; returns GetOverallSignOfChannels().
+template <class T>
+static double channel_run(QubitRegister<T>* q, unsigned long seed, unsigned M, const double* evals,
+                          const double* evecs, const unsigned* qubits, int steps) {
+  using B = typename QubitRegister<T>::BaseType;
+  iqs::RandomNumberGenerator<B> rng;
+  rng.SetSeedStreamPtrs(seed);
+  q->SetRngPtr(&rng);
+  if (M == 4) {
+    GivenChi<T, 4> chi(evals, evecs);
+    for (int i = 0; i < steps; ++i) q->ApplyChannel(qubits[i], chi);
+  } else {
+    GivenChi<T, 16> chi(evals, evecs);
+    for (int i = 0; i < steps; ++i) q->ApplyChannel(qubits[2 * i], qubits[2 * i + 1], chi);
+  }
+  q->ResetRngPtr();
+  return q->GetOverallSignOfChannels();
+}
+extern "C" double ref_channel_run(RefReg* h, unsigned long seed, unsigned M, const double* evals, const double* evecs,
+                                  const unsigned* qubits, int steps) {
+  return h->sp ? channel_run<CSP>(h->spr, seed, M, evals, evecs, qubits, steps)
+               : channel_run<CDP>(h->dp, seed, M, evals, evecs, qubits, steps);
+}
+
+// The reference's unit test ApplyQuantumChannel.IdealHadamard: the eigensystem set by
+// EigensystemOfIdealHadamardChannel (ComplexDP only), ApplyChannel `times` times on `qubit`.
+extern "C" void ref_ideal_hadamard_channel(RefReg* h, unsigned long seed, unsigned qubit, int times) {
+  CM4x4<CDP> chi;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) chi(i, j) = CDP(0, 0);
+  chi(1, 1) = chi(1, 3) = chi(3, 1) = chi(3, 3) = CDP(0.5, 0);
+  chi.EigensystemOfIdealHadamardChannel();
+  iqs::RandomNumberGenerator<double> rng;
+  rng.SetSeedStreamPtrs(seed);
+  h->dp->SetRngPtr(&rng);
+  for (int t = 0; t < times; ++t) h->dp->ApplyChannel(qubit, chi);
+  h->dp->ResetRngPtr();
+}

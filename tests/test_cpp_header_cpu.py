@@ -9,9 +9,14 @@ def test_cpp_header_compiles(tmp_path):
     src.write_text('#include "iqs_gb300/qureg.hpp"\n'
                    "template class iqs::QubitRegister<ComplexDP>;\n"
                    "template class iqs::QubitRegister<ComplexSP>;\n"
+                   "template class iqs::NoisyQureg<ComplexDP>;\n"
+                   "template class iqs::NoisyQureg<ComplexSP>;\n"
+                   "template class iqs::ChiMatrix<ComplexSP, 16, 32>;\n"
                    "int main() { return 0; }\n")
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(REPO / "include"), str(src)], check=True)
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(REPO / "include"),
                     str(REPO / "tests" / "cpp" / "shim_driver.cpp")], check=True)
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(REPO / "include"),
                     str(REPO / "tests" / "cpp" / "qaoa_driver.cpp")], check=True)
+    subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(REPO / "include"),
+                    str(REPO / "tests" / "cpp" / "noise_driver.cpp")], check=True)
