@@ -304,11 +304,22 @@ typedef enum {
                                   applies every gate of a stretch of the stream that acts inside
                                   them, gates on disjoint positions reordered; 0 (default): register
                                   sweeps only. Not used for emulated ComplexDP arithmetic. */
-  IQSG_OPT_NATIVE_SHARE = 3    /* s in 0..16: in emulated-ComplexDP fused sweeps, s/16 of the warps
+  IQSG_OPT_NATIVE_SHARE = 3,   /* s in 0..16: in emulated-ComplexDP fused sweeps, s/16 of the warps
                                   apply their groups in native FP64 (the FP64 pipe) while the rest
                                   use double-float FP32 arithmetic; 0 (default): all emulated.
                                   Results differ from s = 0 only by rounding. */
+  IQSG_OPT_DF_STORAGE = 4      /* 1 (default): an emulated-ComplexDP gate stream of 3+ sweeps whose
+                                  gates are all contractive keeps the state as double-float pairs
+                                  (four floats per amplitude, same 16 bytes) between its sweeps,
+                                  so values are split once and rounded back to FP64 once per call;
+                                  the call still ends with FP64 amplitudes. 0: every sweep reads
+                                  and writes FP64. Results differ by rounding only. */
 } iqsg_option;
+
+/* Counters of a register: [0] double-float storage runs started by iqsg_apply_ops,
+ * [1] kernels those runs launched (one range check and two kernels per sweep, one of which
+ * returns at once). */
+int iqsg_counters(const iqsg_state* h, uint64_t* counters /* [2] */);
 
 /* Set a tuning option. Results depend on it at most by rounding (tile passes reorder gates on
  * disjoint positions; the native share changes which arithmetic a group gets). */

@@ -15,6 +15,9 @@ struct iqsg_state {
   cudaStream_t stream = nullptr;
   bool owns_stream = false;
   int math = IQSG_MATH_NATIVE;
+  bool df_storage = true;  // emulated FP64 runs of sweeps keep double-float pairs between sweeps
+  uint64_t df_runs = 0;      // double-float storage runs started
+  uint64_t df_launches = 0;  // kernels those runs launched
   int device = 0;
   double* scratch = nullptr;      // device: reduction partials + result slots
   double* host_result = nullptr;  // pinned host: reduction results
@@ -35,6 +38,8 @@ constexpr int kMaxPartials = 4096;
 constexpr int kResultSlot = 2 * kMaxPartials;
 // scratch[kErrorSlot] (as unsigned long long): set by a kernel whose bounded wait ran out.
 constexpr int kErrorSlot = 2 * kMaxPartials + 8;
+// scratch[kRangeSlot] (as unsigned long long): set when a double-float storage run may not start.
+constexpr int kRangeSlot = 2 * kMaxPartials + 9;
 // scratch[kTableSlot ...]: small per-call tables (QAOA phases: 2 doubles per cut value).
 constexpr int kTableSlot = 2 * kMaxPartials + 16;
 constexpr int kTableDoubles = 2 * 1040;

@@ -1,5 +1,6 @@
 // Fused-sweep kernel and the scheduler that packs a gate stream into sweeps (iqsg_apply_ops).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -62,9 +63,13 @@ __global__ void __launch_bounds__(kThreads) k_sweep_native(typename V2<R>::type*
 // recomputed in native FP64. Untouched slots are not rewritten. With P.native16 > 0, whole
 // warps (a fixed share of the group blocks) take the native FP64 path from the start, so the
 // FP64 pipe works alongside the FP32 pipes that carry the double-float arithmetic.
+// With only_if set, the kernel runs only when *only_if is nonzero (the state failed the
+// double-float range check of a double-float storage run, see k_sweep_dfs).
 template <int K>
 __global__ void __launch_bounds__(kThreads) k_sweep_df(double2* __restrict__ s, uint64_t ngroups,
-                                                       const __grid_constant__ SweepParams P) {
+                                                       const __grid_constant__ SweepParams P,
+                                                       const unsigned long long* __restrict__ only_if) {
+  if (only_if && !*only_if) return;
   constexpr int G = 1 << K;
   for (uint64_t g = gtid(); g < ngroups; g += gstride()) {
     uint64_t idx[G];
@@ -111,6 +116,88 @@ __global__ void __launch_bounds__(kThreads) k_sweep_df(double2* __restrict__ s, 
 #pragma unroll
     for (int k = 0; k < G; ++k)
       if (tm & (1u << k)) s[idx[k]] = out[k];
+  }
+}
+
+// ---- double-float storage runs ----------------------------------------------------------------
+//
+// A stream of emulated-FP64 sweeps keeps the state as double-float pairs between sweeps: each
+// amplitude's 16 bytes hold (re.h, re.l, im.h, im.l) as four floats instead of two doubles. The
+// first sweep reads FP64 and writes pairs, the middle ones read and write pairs, the last one
+// writes FP64 again, so the split and the rounding back to FP64 happen once per run instead of
+// once per sweep. Every value of the run is a double-float value; where a value fits FP64 this
+// is the same number the per-sweep rounding would store, to within the last of its 53 bits.
+//
+// Range: pairs of floats cover |x| < 2^128, so a run starts only when every component is below
+// 2^77 and finite (k_df_range) and every gate of the run is contractive (checked on the host),
+// which bounds every value of the run by the state's norm. If the check fails on the device,
+// the pair kernels return at once and the IEEE kernel k_sweep_df does each sweep instead.
+
+// Sets *bad when a component is Inf, NaN or at least 2^77 in magnitude.
+__global__ void __launch_bounds__(kThreads) k_df_range(const double2* __restrict__ s, uint64_t n,
+                                                       unsigned long long* __restrict__ bad) {
+  bool b = false;
+  for (uint64_t i = gtid(); i < n; i += gstride()) {
+    const double2 v = s[i];
+    const uint32_t ex = (uint32_t)(df64::d2u(v.x) >> 52) & 0x7FFu, ey = (uint32_t)(df64::d2u(v.y) >> 52) & 0x7FFu;
+    b |= (ex >= df64::kEmax) | (ey >= df64::kEmax);
+  }
+  if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31u) == 0u) atomicOr(bad, 1ull);
+}
+
+// FP64 -> pair. Below the split's fast range (|x| < 2^-73) the float conversions are used.
+__device__ __forceinline__ df64::DF split_any(double x) {
+  df64::DF r;
+  if (!df64::split(x, r)) {
+    r.h = __double2float_rn(x);
+    r.l = __double2float_rn(x - (double)r.h);
+  }
+  return r;
+}
+
+// Pair -> nearest FP64; outside merge's fast range the sum is formed in FP64.
+__device__ __forceinline__ double merge_any(const df64::DF& a) {
+  double d;
+  if (!df64::merge(a.h, a.l, d)) d = (double)a.h + (double)a.l;
+  return d;
+}
+
+template <int K, bool IN_PAIRS, bool OUT_PAIRS>
+__global__ void __launch_bounds__(kThreads) k_sweep_dfs(double2* __restrict__ s, uint64_t ngroups,
+                                                        const __grid_constant__ SweepParams P,
+                                                        const unsigned long long* __restrict__ bad) {
+  if (*bad) return;
+  constexpr int G = 1 << K;
+  // A sweep that changes the format rewrites every slot; one that keeps it, only touched ones.
+  constexpr bool kAll = IN_PAIRS != OUT_PAIRS;
+  float4* f = reinterpret_cast<float4*>(s);
+  for (uint64_t g = gtid(); g < ngroups; g += gstride()) {
+    uint64_t idx[G];
+    group_indices<K>(P, g, idx);
+    DF64Arith::VT v[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      if constexpr (IN_PAIRS) {
+        const float4 t = f[idx[k]];
+        v[k].re = df64::DF{t.x, t.y};
+        v[k].im = df64::DF{t.z, t.w};
+      } else {
+        const double2 t = s[idx[k]];
+        v[k].re = split_any(t.x);
+        v[k].im = split_any(t.y);
+      }
+    }
+    unsigned tm = 0;
+    run_ops<DF64Arith, K>(P, v, idx, tm);
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      if (!kAll && !(tm & (1u << k))) continue;
+      if constexpr (OUT_PAIRS) {
+        f[idx[k]] = make_float4(v[k].re.h, v[k].re.l, v[k].im.h, v[k].im.l);
+      } else {
+        s[idx[k]] = make_double2(merge_any(v[k].re), merge_any(v[k].im));
+      }
+    }
   }
 }
 
@@ -432,7 +519,7 @@ void launch_k(iqsg_state* h, const SweepParams& P) {
     k_sweep_native<float, K><<<grid, kThreads, 0, h->stream>>>(reinterpret_cast<float2*>(h->amps), ngroups, P);
   } else if (df) {
     if constexpr (K <= 3) {
-      k_sweep_df<K><<<grid, kThreads, 0, h->stream>>>(reinterpret_cast<double2*>(h->amps), ngroups, P);
+      k_sweep_df<K><<<grid, kThreads, 0, h->stream>>>(reinterpret_cast<double2*>(h->amps), ngroups, P, nullptr);
     }
   } else {
     k_sweep_native<double, K><<<grid, kThreads, 0, h->stream>>>(reinterpret_cast<double2*>(h->amps), ngroups, P);
@@ -440,6 +527,42 @@ void launch_k(iqsg_state* h, const SweepParams& P) {
 }
 
 }  // namespace
+
+namespace {
+
+// One sweep of a double-float storage run: the pair kernel, and the IEEE kernel that runs in
+// its place when the range check failed.
+template <int K>
+void launch_dfs_k(iqsg_state* h, const SweepParams& P, bool first, bool last) {
+  if constexpr (K <= 3) {
+    const uint64_t ngroups = h->N >> K;
+    const unsigned grid = grid_for(ngroups, 1);
+    double2* s = reinterpret_cast<double2*>(h->amps);
+    const auto* bad = reinterpret_cast<const unsigned long long*>(h->scratch + kRangeSlot);
+    if (first && last) k_sweep_dfs<K, false, false><<<grid, kThreads, 0, h->stream>>>(s, ngroups, P, bad);
+    else if (first) k_sweep_dfs<K, false, true><<<grid, kThreads, 0, h->stream>>>(s, ngroups, P, bad);
+    else if (last) k_sweep_dfs<K, true, false><<<grid, kThreads, 0, h->stream>>>(s, ngroups, P, bad);
+    else k_sweep_dfs<K, true, true><<<grid, kThreads, 0, h->stream>>>(s, ngroups, P, bad);
+    k_sweep_df<K><<<grid, kThreads, 0, h->stream>>>(s, ngroups, P, bad);
+  }
+}
+
+}  // namespace
+
+void launch_df_storage_run(iqsg_state* h, const std::vector<SweepParams>& progs) {
+  auto* bad = reinterpret_cast<unsigned long long*>(h->scratch + kRangeSlot);
+  cudaMemsetAsync(bad, 0, sizeof(unsigned long long), h->stream);
+  k_df_range<<<grid_for(h->N, 1), kThreads, 0, h->stream>>>(reinterpret_cast<const double2*>(h->amps), h->N, bad);
+  for (size_t i = 0; i < progs.size(); ++i) {
+    const bool first = i == 0, last = i + 1 == progs.size();
+    switch (progs[i].K) {
+      case 0: launch_dfs_k<0>(h, progs[i], first, last); break;
+      case 1: launch_dfs_k<1>(h, progs[i], first, last); break;
+      case 2: launch_dfs_k<2>(h, progs[i], first, last); break;
+      case 3: launch_dfs_k<3>(h, progs[i], first, last); break;
+    }
+  }
+}
 
 void launch_sweep(iqsg_state* h, const SweepParams& P) {
   switch (P.K) {
@@ -525,6 +648,9 @@ extern "C" int iqsg_set_option(iqsg_state* h, int option, int value) {
       if (value < 0 || value > 16) return fail(IQSG_EINVAL, "iqsg_set_option: native share %d outside 0..16", value);
       h->native16 = (unsigned)value;
       return IQSG_OK;
+    case IQSG_OPT_DF_STORAGE:
+      h->df_storage = value != 0;
+      return IQSG_OK;
     case IQSG_OPT_TILE_QUBITS:
       if (value < 0 || value > 14) return fail(IQSG_EINVAL, "iqsg_set_option: tile size %d outside 0..14", value);
       h->tile_qubits = (unsigned)value;
@@ -533,6 +659,53 @@ extern "C" int iqsg_set_option(iqsg_state* h, int option, int value) {
       return fail(IQSG_EINVAL, "iqsg_set_option: unknown option %d", option);
   }
 }
+
+namespace {
+
+// Sweeps a double-float storage run needs at least: the range check costs about a fifth of a
+// sweep, and each sweep between the first and the last saves about a third of one.
+constexpr size_t kDfStoreMinSweeps = 3;
+
+// Upper bound of the spectral norm of an op on the whole space (identity outside its block):
+// the square root of the largest Gershgorin row sum of M^H M.
+double op_norm_bound(const iqsg_op& op) {
+  auto gersh = [](const double* m, int d) {
+    double best = 0;
+    for (int i = 0; i < d; ++i) {
+      double rs = 0;
+      for (int j = 0; j < d; ++j) {
+        double re = 0, im = 0;  // (M^H M)_ij = sum_k conj(M_ki) M_kj
+        for (int k = 0; k < d; ++k) {
+          const double ar = m[2 * (k * d + i)], ai = m[2 * (k * d + i) + 1];
+          const double br = m[2 * (k * d + j)], bi = m[2 * (k * d + j) + 1];
+          re += ar * br + ai * bi;
+          im += ar * bi - ai * br;
+        }
+        rs += std::sqrt(re * re + im * im);
+      }
+      best = std::max(best, rs);
+    }
+    return std::sqrt(best);
+  };
+  auto absc = [](const double* z) { return std::sqrt(z[0] * z[0] + z[1] * z[1]); };
+  switch (op.kind) {
+    case IQSG_OP_1Q: return gersh(op.m, 2);
+    case IQSG_OP_CTRL:
+    case IQSG_OP_SWAPLIKE: return std::max(1.0, gersh(op.m, 2));
+    case IQSG_OP_2Q: return gersh(op.m, 4);
+    case IQSG_OP_DIAG2: return std::max(std::max(absc(op.m), absc(op.m + 2)), std::max(absc(op.m + 4), absc(op.m + 6)));
+    case IQSG_OP_PHASE: return std::max(1.0, absc(op.m));
+    default: return HUGE_VAL;
+  }
+}
+
+class CollectSweeps : public SweepSink {
+ public:
+  void take(const SweepParams& P, const GradMap&) override { progs.push_back(P); }
+  std::vector<SweepParams> progs;
+};
+
+}  // namespace
 
 extern "C" int iqsg_apply_ops(iqsg_state* h, const iqsg_op* ops, unsigned count, unsigned* sweeps) {
   if (!h) return fail(IQSG_EINVAL, "null register handle");
@@ -544,11 +717,40 @@ extern "C" int iqsg_apply_ops(iqsg_state* h, const iqsg_op* ops, unsigned count,
   const bool df = h->prec == IQSG_COMPLEX_DP && h->math == IQSG_MATH_EMULATED;
   const unsigned kt = df ? 0u : tile_qubits(h, false);
   if (kt) return tile_schedule(h, nullptr, ops, count, kt, std::max(1u, sweep_width(h)), nullptr, sweeps);
+  if (df && h->df_storage && !h->bulk && h->native16 == 0 && h->n >= 2) {
+    // Emulated FP64: collect the sweeps, then run them with the state as double-float pairs
+    // when the run is long enough and every gate is contractive.
+    CollectSweeps c;
+    {
+      SweepBuilder b(&c, std::max(1u, sweep_width(h)));
+      for (unsigned i = 0; i < count; ++i) queue_op(b, ops[i]);
+      b.flush();
+    }
+    bool pairs = c.progs.size() >= kDfStoreMinSweeps;
+    for (unsigned i = 0; pairs && i < count; ++i) pairs = op_norm_bound(ops[i]) <= 1.0 + 1e-9;
+    for (const auto& P : c.progs) pairs = pairs && P.K <= 3;
+    if (pairs) {
+      launch_df_storage_run(h, c.progs);
+      h->df_runs += 1;
+      h->df_launches += 1 + 2 * c.progs.size();
+    } else {
+      for (auto& P : c.progs) launch_sweep(h, P);
+    }
+    if (sweeps) *sweeps = (unsigned)c.progs.size();
+    return cuda_status(cudaGetLastError(), "iqsg_apply_ops");
+  }
   SweepBuilder b(h, std::max(1u, sweep_width(h)));
   for (unsigned i = 0; i < count; ++i) queue_op(b, ops[i]);
   b.flush();
   if (sweeps) *sweeps = b.launched();
   return cuda_status(cudaGetLastError(), "iqsg_apply_ops");
+}
+
+extern "C" int iqsg_counters(const iqsg_state* h, uint64_t* counters) {
+  if (!h || !counters) return fail(IQSG_EINVAL, "iqsg_counters: null argument");
+  counters[0] = h->df_runs;
+  counters[1] = h->df_launches;
+  return IQSG_OK;
 }
 
 extern "C" int iqsg_adjoint_ops(iqsg_state* psi, iqsg_state* lam, const iqsg_op* ops, unsigned count, double* grads,

@@ -11,6 +11,8 @@
 // operation of the sweep.
 #pragma once
 
+#include <vector>
+
 #include "df64.cuh"
 #include "iqsg_internal.cuh"
 
@@ -523,6 +525,8 @@ __device__ __forceinline__ void run_ops_dual(const SweepParams& P, typename Nati
 
 // Host side: launch one sweep on the register (k_sweep.cu).
 void launch_sweep(iqsg_state* h, const SweepParams& P);
+// Emulated-FP64 sweeps with the state held as double-float pairs between them (k_sweep.cu).
+void launch_df_storage_run(iqsg_state* h, const std::vector<SweepParams>& progs);
 
 // Host side: one adjoint sweep over psi and lam; gradient slot s adds into grad[param[s]]
 // (a device array of doubles).

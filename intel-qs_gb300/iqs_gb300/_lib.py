@@ -15,7 +15,7 @@ LIB_PATH = _HERE / "libiqsg.so"
 IQSG_OK, IQSG_EINVAL, IQSG_ENOMEM, IQSG_EDEVICE, IQSG_ETIMEOUT, IQSG_ENOTSUP = range(6)
 COMPLEX_DP, COMPLEX_SP = 0, 1
 MATH_NATIVE, MATH_EMULATED = 0, 1
-OPT_SWEEP_WIDTH, OPT_SWEEP_PIPELINE, OPT_TILE_QUBITS, OPT_NATIVE_SHARE = 0, 1, 2, 3
+OPT_SWEEP_WIDTH, OPT_SWEEP_PIPELINE, OPT_TILE_QUBITS, OPT_NATIVE_SHARE, OPT_DF_STORAGE = 0, 1, 2, 3, 4
 
 _P = C.c_void_p
 _U = C.c_uint
@@ -64,6 +64,7 @@ SIGNATURES = {
     "iqsg_upload": [_P, _P, _U64, _U64],
     "iqsg_download": [_P, _P, _U64, _U64],
     "iqsg_init_uniform_random": [_P, _U64, _U64, _D, _D],
+    "iqsg_counters": [_P, C.POINTER(_U64)],
     "iqsg_rng_create": [C.POINTER(_P)],
     "iqsg_rng_destroy": [_P],
     "iqsg_rng_clone": [_P, C.c_int, C.POINTER(_P)],

@@ -466,6 +466,18 @@ class QubitRegister:
         self._flush()
         check(lib.iqsg_set_option(self._h, _lib.OPT_NATIVE_SHARE, int(sixteenths)))
 
+    def SetDoubleFloatStorage(self, on: bool) -> None:
+        """Emulated ComplexDP gate streams of 3+ sweeps: keep the state as double-float pairs
+        between sweeps (default on); off, every sweep reads and writes FP64. Rounding only."""
+        self._flush()
+        check(lib.iqsg_set_option(self._h, _lib.OPT_DF_STORAGE, 1 if on else 0))
+
+    def counters(self) -> dict:
+        """Double-float storage runs started by fused gate streams and the kernels they launched."""
+        c = (C.c_uint64 * 2)()
+        check(lib.iqsg_counters(self._h, c))
+        return {"df_runs": int(c[0]), "df_launches": int(c[1])}
+
     def SetTileQubits(self, k: int) -> None:
         """Run fused gate streams as shared-memory tile passes spanning k positions (0 = off,
         register sweeps only); a tuning choice that changes results only by rounding (gates
