@@ -145,25 +145,46 @@ __global__ void __launch_bounds__(kThreads) k_df_range(const double2* __restrict
   if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31u) == 0u) atomicOr(bad, 1ull);
 }
 
-// FP64 -> pair. Below the split's fast range (|x| < 2^-73) the float conversions are used.
-__device__ __forceinline__ df64::DF split_any(double x) {
-  df64::DF r;
-  if (!df64::split(x, r)) {
-    r.h = __double2float_rn(x);
-    r.l = __double2float_rn(x - (double)r.h);
+// FP64 -> pairs for the values the integer split does not take (|x| < 2^-73, the range check
+// having excluded large ones), and pairs -> FP64 where the integer rounding does not apply.
+// Called under a warp-uniform branch, so the fast path does not issue their FP64
+// instructions predicated off.
+template <int G>
+__device__ __forceinline__ void split_slow(const double2* raw, DF64Arith::VT* v) {
+#pragma unroll
+  for (int k = 0; k < G; ++k) {
+    v[k].re.h = __double2float_rn(raw[k].x);
+    v[k].re.l = __double2float_rn(raw[k].x - (double)v[k].re.h);
+    v[k].im.h = __double2float_rn(raw[k].y);
+    v[k].im.l = __double2float_rn(raw[k].y - (double)v[k].im.h);
   }
-  return r;
+}
+template <int G>
+__device__ __forceinline__ void merge_slow(const DF64Arith::VT* v, double2* out) {
+#pragma unroll
+  for (int k = 0; k < G; ++k) {
+    out[k].x = (double)v[k].re.h + (double)v[k].re.l;
+    out[k].y = (double)v[k].im.h + (double)v[k].im.l;
+  }
 }
 
-// Pair -> nearest FP64; outside merge's fast range the sum is formed in FP64.
-__device__ __forceinline__ double merge_any(const df64::DF& a) {
-  double d;
-  if (!df64::merge(a.h, a.l, d)) d = (double)a.h + (double)a.l;
-  return d;
+// Resident blocks per SM the pair kernels are compiled for (register budget), by width. On
+// GB300 (30-qubit layer): width 2 is fastest at 4 blocks (64 registers; 48 registers with 5
+// blocks spill and lose 4 %); width 3 gains 24 % at 3 blocks (80 registers, 64 bytes of
+// spills) over 2 blocks (128 registers).
+#ifndef IQSG_DFS_MIN_BLOCKS_K2
+#define IQSG_DFS_MIN_BLOCKS_K2 4
+#endif
+#ifndef IQSG_DFS_MIN_BLOCKS_K3
+#define IQSG_DFS_MIN_BLOCKS_K3 3
+#endif
+template <int K>
+constexpr int dfs_min_blocks() {
+  return K == 3 ? IQSG_DFS_MIN_BLOCKS_K3 : (K == 2 ? IQSG_DFS_MIN_BLOCKS_K2 : 1);
 }
 
 template <int K, bool IN_PAIRS, bool OUT_PAIRS>
-__global__ void __launch_bounds__(kThreads) k_sweep_dfs(double2* __restrict__ s, uint64_t ngroups,
+__global__ void __launch_bounds__(kThreads, dfs_min_blocks<K>()) k_sweep_dfs(double2* __restrict__ s, uint64_t ngroups,
                                                         const __grid_constant__ SweepParams P,
                                                         const unsigned long long* __restrict__ bad) {
   if (*bad) return;
@@ -175,28 +196,46 @@ __global__ void __launch_bounds__(kThreads) k_sweep_dfs(double2* __restrict__ s,
     uint64_t idx[G];
     group_indices<K>(P, g, idx);
     DF64Arith::VT v[G];
+    if constexpr (IN_PAIRS) {
 #pragma unroll
-    for (int k = 0; k < G; ++k) {
-      if constexpr (IN_PAIRS) {
+      for (int k = 0; k < G; ++k) {
         const float4 t = f[idx[k]];
         v[k].re = df64::DF{t.x, t.y};
         v[k].im = df64::DF{t.z, t.w};
-      } else {
-        const double2 t = s[idx[k]];
-        v[k].re = split_any(t.x);
-        v[k].im = split_any(t.y);
+      }
+    } else {
+      double2 raw[G];
+      bool ok = true;
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        raw[k] = s[idx[k]];
+        ok &= df64::split(raw[k].x, v[k].re);
+        ok &= df64::split(raw[k].y, v[k].im);
+      }
+      if (__builtin_expect(__any_sync(__activemask(), !ok), 0)) {
+        if (!ok) split_slow<G>(raw, v);
       }
     }
     unsigned tm = 0;
     run_ops<DF64Arith, K>(P, v, idx, tm);
+    if constexpr (OUT_PAIRS) {
 #pragma unroll
-    for (int k = 0; k < G; ++k) {
-      if (!kAll && !(tm & (1u << k))) continue;
-      if constexpr (OUT_PAIRS) {
-        f[idx[k]] = make_float4(v[k].re.h, v[k].re.l, v[k].im.h, v[k].im.l);
-      } else {
-        s[idx[k]] = make_double2(merge_any(v[k].re), merge_any(v[k].im));
+      for (int k = 0; k < G; ++k)
+        if (kAll || (tm & (1u << k))) f[idx[k]] = make_float4(v[k].re.h, v[k].re.l, v[k].im.h, v[k].im.l);
+    } else {
+      double2 out[G];
+      bool ok = true;
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        ok &= df64::merge(v[k].re.h, v[k].re.l, out[k].x);
+        ok &= df64::merge(v[k].im.h, v[k].im.l, out[k].y);
       }
+      if (__builtin_expect(__any_sync(__activemask(), !ok), 0)) {
+        if (!ok) merge_slow<G>(v, out);
+      }
+#pragma unroll
+      for (int k = 0; k < G; ++k)
+        if (kAll || (tm & (1u << k))) s[idx[k]] = out[k];
     }
   }
 }
