@@ -407,9 +407,10 @@ def gate_bytes(ops, n: int, amp_bytes: int) -> int:
 
 
 def qft_brick_section(n: int = 30, layers: int = 40) -> dict:
-    """QFT + 40 Haar/CZ brick layers from a seeded basis state: ComplexDP gate by gate
-    (emulated arithmetic), ComplexSP in fused passes; errors against the amplitudes the
-    reference itself computed (tests/golden/qft_brick.npz) and SP fidelity against DP."""
+    """QFT + 40 Haar/CZ brick layers from a seeded basis state: ComplexDP gate by gate and in
+    fused passes (emulated arithmetic), ComplexSP in fused passes; errors against the
+    amplitudes the reference itself computed (tests/golden/qft_brick.npz), SP fidelity
+    against DP."""
     import hashlib
     import torch
     import iqs_gb300 as iqs
@@ -448,6 +449,12 @@ def qft_brick_section(n: int = 30, layers: int = 40) -> dict:
 
     dp = iqs.QubitRegister(n, "base", start, precision="DP", math="emulated")
     t_dp, _ = timed(dp, False)
+    dpf = iqs.QubitRegister(n, "base", start, precision="DP", math="emulated")
+    t_dpf, sweeps_dpf = timed(dpf, True)
+    dpf_runs = dpf.counters()["df_runs"]
+    dpf_err = sample_err(dpf)
+    dpf_diff = float((torch.as_tensor(dpf, device="cuda") - torch.as_tensor(dp, device="cuda")).abs().max())
+    del dpf
     sp = iqs.QubitRegister(n, "base", start, precision="SP")
     t_sp, sweeps = timed(sp, True)
     sp.Initialize("base", start)
@@ -464,6 +471,9 @@ def qft_brick_section(n: int = 30, layers: int = 40) -> dict:
         "dp_gate_by_gate": {"s": round(t_dp, 3), "launches": len(ops),
                             "gbs_algorithmic": round(gate_bytes(ops, n, 16) / t_dp / 1e9, 1),
                             "max_abs_err_vs_reference_sample": sample_err(dp)},
+        "dp_fused": {"s": round(t_dpf, 3), "passes": sweeps_dpf, "double_float_storage_runs": dpf_runs,
+                     "gbs_algorithmic": round(gate_bytes(ops, n, 16) / t_dpf / 1e9, 1),
+                     "max_abs_err_vs_reference_sample": dpf_err, "max_abs_diff_vs_dp_gate_by_gate": dpf_diff},
         "sp_fused": {"s": round(t_sp, 3), "passes": sweeps,
                      "gbs_algorithmic": round(gate_bytes(ops, n, 8) / t_sp / 1e9, 1),
                      "max_abs_err_vs_reference_sample": sample_err(sp),
@@ -674,66 +684,88 @@ def run_ours(args) -> None:
     # DRAM bytes per launch: given on the command line, else the ratio ncu measured for the
     # fused emulated pass on a 27-qubit state (4.234 GB read + written per 4.295 GB pass; the
     # capture is too large to repeat at 30 qubits), scaled by the amplitudes of this pass.
+    width_used = args.width or (tuned and tuned["width"])
     if args.traffic is not None:
         traffic, traffic_src = args.traffic, "command line"
-    elif args.fusion and args.math == "emulated" and not df_runs and (args.width or (tuned and tuned["width"])) == 2:
+    elif args.fusion and args.math == "emulated" and df_runs and width_used == 2:
+        # ncu on k_sweep_dfs<2, pairs in, pairs out> at 27 qubits: 4.234 GB per 4.295 GB pass.
+        traffic = round(4.234e9 / 4.295e9 * 2 * (1 << n) * 16)
+        traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_sweep_dfs<2,1,1> at 27 qubits, scaled"
+    elif args.fusion and args.math == "emulated" and not df_runs and width_used == 2:
         traffic = round(4.234e9 / 4.295e9 * 2 * (1 << n) * 16)
         traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_sweep_df<2> at 27 qubits, scaled"
     else:
         traffic, traffic_src = None, None
 
     # End to end through the public API with host buffers: every step uploads its input from
-    # pinned host memory, applies the layer and downloads its result. With room for two
-    # pinned state buffers, two registers on two streams take alternate steps, so one step's
-    # copies overlap the other register's layer (the copies are queued with
-    # SetStateVectorAsync / GetStateVectorAsync in stream order with the gates).
+    # pinned host memory, applies the layer and downloads its result. With room for more
+    # pinned state buffers, up to three registers on their own streams take turns as a
+    # three-stage pipeline: uploads run one after another in issue order, so do the layers and
+    # the downloads (cross-stream events), so one register's upload, another's layer and a
+    # third's download overlap instead of splitting each engine between them. The copies are
+    # SetStateVectorAsync / GetStateVectorAsync, queued in stream order with the gates.
     state_bytes = (1 << n) * 16
-    pipelined = host_mem_available() >= 3 * state_bytes + (16 << 30)
-    regs, hosts = [reg], []
-    if pipelined:
-        stream2 = torch.cuda.Stream()
-        reg2 = iqs.QubitRegister(n, "", 0, math=args.math, stream=stream2.cuda_stream)
+    avail = host_mem_available()
+    nreg = 3 if avail >= 4 * state_bytes + (16 << 30) else (2 if avail >= 3 * state_bytes + (16 << 30) else 1)
+    regs, hosts, streams = [reg], [], [stream]
+    for _ in range(1, nreg):
+        st_ = torch.cuda.Stream()
+        r2 = iqs.QubitRegister(n, "", 0, math=args.math, stream=st_.cuda_stream)
         if args.width:
-            reg2.SetSweepWidth(args.width)
-            reg2.SetSweepPipeline(args.pipeline)
+            r2.SetSweepWidth(args.width)
+            r2.SetSweepPipeline(args.pipeline)
             if args.math == "emulated":
-                reg2.SetNativeShare(args.native_share)
+                r2.SetNativeShare(args.native_share)
         elif tuned:
-            reg2.SetSweepWidth(tuned["width"])
-            reg2.SetSweepPipeline(tuned["pipeline"])
+            r2.SetSweepWidth(tuned["width"])
+            r2.SetSweepPipeline(tuned["pipeline"])
             if args.math == "emulated":
-                reg2.SetNativeShare(tuned["native_share"])
+                r2.SetNativeShare(tuned["native_share"])
         if args.fusion:
-            reg2.TurnOnFusion()
-        regs.append(reg2)
+            r2.TurnOnFusion()
+        regs.append(r2)
+        streams.append(st_)
     for r_ in regs:
         h_ = torch.empty(1 << n, dtype=torch.complex128, pin_memory=True)  # the tensor keeps the pinned block
         reg.GetStateVector(out=h_.numpy())
         hosts.append(h_)
-    e2e_steps = max(2 * len(regs), min(args.steps, 6))
+    e2e_steps = min(max(4 * nreg, args.steps), 12)
+    last = {"up": None, "layer": None, "down": None}
 
-    def e2e_step(r_, hb, s):
-        r_.SetStateVectorAsync(hb.numpy())            # host (pinned) -> HBM
-        apply_layer(r_, mats[s], n)
-        r_.ApplyFusedGates()
-        r_.GetStateVectorAsync(hb.numpy())            # HBM -> host (pinned)
+    def stage(st_, key, fn):
+        if last[key] is not None:
+            st_.wait_event(last[key])
+        fn()
+        ev = torch.cuda.Event()
+        ev.record(st_)
+        last[key] = ev
 
-    for i_, r_ in enumerate(regs):                    # untimed: first use of each buffer and stream
-        e2e_step(r_, hosts[i_], args.warmup)
+    def e2e_step(i, s):
+        r_, hb, st_ = regs[i], hosts[i], streams[i]
+
+        def layer():
+            apply_layer(r_, mats[s], n)
+            r_.ApplyFusedGates()
+        stage(st_, "up", lambda: r_.SetStateVectorAsync(hb.numpy()))     # host (pinned) -> HBM
+        stage(st_, "layer", layer)
+        stage(st_, "down", lambda: r_.GetStateVectorAsync(hb.numpy()))   # HBM -> host (pinned)
+
+    for i_ in range(nreg):                            # untimed: first use of each buffer and stream
+        e2e_step(i_, args.warmup)
     for r_ in regs:
         r_.synchronize()
     barrier()
     t0 = time.perf_counter()
     for s in range(e2e_steps):
-        e2e_step(regs[s % len(regs)], hosts[s % len(regs)], args.warmup + s % args.steps)
+        e2e_step(s % nreg, args.warmup + s % args.steps)
     for r_ in regs:
         r_.synchronize()
     barrier()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dist)
     e2e_value = job_gbs(world, layer_bytes(n), e2e_s)
     del hosts
-    if pipelined:
-        del regs[1], reg2
+    del regs[1:]
+    pipelined = nreg
 
     # Same layer with native FP64 arithmetic, for comparison (2 steps).
     other = {}
@@ -812,7 +844,8 @@ def run_ours(args) -> None:
                          "traffic": traffic, "traffic_source": traffic_src},
             "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": (1 << n) * 16,
                     "d2h_bytes_per_step": (1 << n) * 16, "steps": e2e_steps,
-                    "path": ("two registers on two streams take alternate steps: " if pipelined else "") +
+                    "path": (f"{pipelined} registers on their own streams take turns as a three-stage pipeline "
+                             "(uploads, layers and downloads each in issue order): " if pipelined > 1 else "") +
                             "QubitRegister.SetStateVectorAsync (pinned host) + layer via the public API + "
                             "GetStateVectorAsync (pinned host), wall clock over all steps"},
             "gpu_launches": launches,
