@@ -698,3 +698,4 @@ template <class Type>
 using TM4x4 = iqs::TinyMatrix<Type, 4, 4, 32>;
 
 #include "noisy_qureg.hpp"
+#include "qubit_register_metric.hpp"

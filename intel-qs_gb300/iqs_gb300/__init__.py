@@ -15,7 +15,7 @@ from .adjoint import QaoaMaxCut, qaoa_energy
 from .batched import BatchedAnsatz
 from .rng import RandomNumberGenerator
 from .chi import CM4x4, CM16x16, ChiMatrix
-from .noisy import NoisyQureg
+from .noisy import NoisyQureg, QubitRegisterMetric
 from .trotter import XXZChain
 from .qaoa import (GetExpectationValueFromCostFunction, GetExpectationValueSquaredFromCostFunction,
                    GetHistogramFromCostFunction, GetHistogramFromCostFunctionWithWeightsBinned,
@@ -28,5 +28,5 @@ __all__ = [
     "GetExpectationValueFromCostFunction", "GetExpectationValueSquaredFromCostFunction",
     "InitializeVectorAsWeightedMaxCutCostFunction", "GetHistogramFromCostFunction",
     "GetHistogramFromCostFunctionWithWeightsRounded", "GetHistogramFromCostFunctionWithWeightsBinned",
-    "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz", "XXZChain", "RandomNumberGenerator", "ChiMatrix", "CM4x4", "CM16x16", "NoisyQureg",
+    "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz", "XXZChain", "RandomNumberGenerator", "ChiMatrix", "CM4x4", "CM16x16", "NoisyQureg", "QubitRegisterMetric",
 ]

@@ -172,3 +172,62 @@ for _name in ("ApplyPauliX", "ApplyPauliY", "ApplyPauliZ", "ApplyPauliSqrtX", "A
     if hasattr(QubitRegister, _name):
         setattr(NoisyQureg, _name, _plain(_name))
 del _name
+
+
+class QubitRegisterMetric(QubitRegister):
+    """QubitRegisterMetric (include/QubitRegisterMetric.hpp): the gates below also count 1- and
+    2-qubit gates and track a per-qubit depth (a 2-qubit gate puts both qubits at one more than
+    the deeper of the two). Other gates are not counted, as in the reference."""
+
+    def __init__(self, num_qubits: int, *, precision: str = "DP", math: str = "native"):
+        super().__init__(num_qubits, "", 0, precision=precision, math=math)
+        self._total = self._one = self._two = 0
+        self._depth = [0] * num_qubits
+        self._inside = False
+
+    def GetTotalQubitGateCount(self) -> int:
+        return self._total
+
+    def GetOneQubitGateCount(self) -> int:
+        return self._one
+
+    def GetTwoQubitGateCount(self) -> int:
+        return self._two
+
+    def GetParallelDepth(self) -> int:
+        return max(self._depth) if self._depth else 0
+
+    def _count(self, base, qs, *args):
+        if self._inside:  # a counted gate built from another counted one counts once
+            return base(self, *args)
+        self._inside = True
+        try:
+            base(self, *args)
+        finally:
+            self._inside = False
+        self._total += 1
+        if len(qs) == 1:
+            self._one += 1
+            self._depth[qs[0]] += 1
+        else:
+            self._two += 1
+            d = max(self._depth[qs[0]], self._depth[qs[1]]) + 1
+            self._depth[qs[0]] = self._depth[qs[1]] = d
+
+    def ApplyHadamard(self, q: int) -> None:
+        self._count(QubitRegister.ApplyHadamard, (q,), q)
+
+    def ApplyRotationX(self, q: int, theta: float) -> None:
+        self._count(QubitRegister.ApplyRotationX, (q,), q, theta)
+
+    def ApplyRotationY(self, q: int, theta: float) -> None:
+        self._count(QubitRegister.ApplyRotationY, (q,), q, theta)
+
+    def ApplyRotationZ(self, q: int, theta: float) -> None:
+        self._count(QubitRegister.ApplyRotationZ, (q,), q, theta)
+
+    def ApplyCPauliX(self, q1: int, q2: int) -> None:
+        self._count(QubitRegister.ApplyCPauliX, (q1, q2), q1, q2)
+
+    def ApplyControlled1QubitGate(self, q1: int, q2: int, m, *args, **kw) -> None:
+        self._count(lambda s, *a: QubitRegister.ApplyControlled1QubitGate(s, *a, **kw), (q1, q2), q1, q2, m, *args)

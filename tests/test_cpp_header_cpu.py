@@ -10,6 +10,8 @@ def test_cpp_header_compiles(tmp_path):
                    "template class iqs::QubitRegister<ComplexDP>;\n"
                    "template class iqs::QubitRegister<ComplexSP>;\n"
                    "template class iqs::NoisyQureg<ComplexDP>;\n"
+                   "template class iqs::QubitRegisterMetric<ComplexDP>;\n"
+                   "template class iqs::QubitRegisterMetric<ComplexSP>;\n"
                    "template class iqs::NoisyQureg<ComplexSP>;\n"
                    "template class iqs::ChiMatrix<ComplexSP, 16, 32>;\n"
                    "int main() { return 0; }\n")

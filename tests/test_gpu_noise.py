@@ -281,3 +281,23 @@ def test_cpp_channels_match_reference(noise_driver, key):
     scale = max(1.0, float(np.max(np.abs(want))))
     assert np.max(np.abs(_state(out, n) - want)) <= TOL[prec] * 10 * scale
     assert float(out[1 << n].split()[1]) == float(z[f"{key}/sign"])
+
+
+def test_qubit_register_metric_counts_and_depth():
+    """QubitRegisterMetric (include/QubitRegisterMetric.hpp): counts and parallel depth of the
+    counted gates; the state equals a plain register's."""
+    import iqs_gb300 as iqs
+    r = iqs.QubitRegisterMetric(4)
+    r.Initialize("base", 0)
+    plain = iqs.QubitRegister(4, "base", 0)
+    for reg in (r, plain):
+        reg.ApplyHadamard(0)
+        reg.ApplyRotationX(1, 0.3)
+        reg.ApplyCPauliX(0, 1)
+        reg.ApplyRotationZ(3, 1.1)
+        reg.ApplyControlled1QubitGate(1, 2, np.array([[0, 1], [1, 0]], dtype=complex))
+        reg.ApplyPauliY(3)  # not counted
+    assert (r.GetOneQubitGateCount(), r.GetTwoQubitGateCount(), r.GetTotalQubitGateCount()) == (3, 2, 5)
+    # depths: q0 1 -> 2 (CX with q1 at 1), q1 -> 2 -> 3 (CU with q2 at 0), q2 -> 3, q3 -> 1
+    assert r.GetParallelDepth() == 3
+    assert np.max(np.abs(r.GetStateVector() - plain.GetStateVector())) <= 1e-15
