@@ -86,3 +86,89 @@ def test_merge_is_nearest_double(df64_results):
 def test_gate_row_error_bound(df64_results):
     """A 4-term complex-gate row: error below 2^-44 of the sum of |terms|."""
     assert df64_results[3] <= 2.0 ** -44
+
+
+CHAIN = r"""
+#include <complex>
+#include <cstdio>
+#include <cmath>
+#include <random>
+#include <vector>
+#include "df64.cuh"
+using namespace df64;
+using LC = std::complex<long double>;
+struct CDF { DF re, im; };
+// One 2x2 row (m0 a + m1 b) in double-float: four exact products per component, TwoSum sums.
+static DF dot4(const DF* c, const DF* x, const float* sgn) {
+  Acc s; float ph, pl;
+  for (int k = 0; k < 4; ++k) {
+    prod(sgn[k] * c[k].h, sgn[k] * c[k].l, x[k].h, x[k].l, ph, pl);
+    if (k == 0) acc_init(s, ph, pl); else acc_add(s, ph, pl);
+  }
+  DF r; acc_norm(s, r.h, r.l); return r;
+}
+static CDF row(const CDF& m0, const CDF& m1, const CDF& a, const CDF& b) {
+  const DF cr[4] = {m0.re, m0.im, m1.re, m1.im};
+  const float sr[4] = {1, -1, 1, -1}, si[4] = {1, 1, 1, 1};
+  const DF xr[4] = {a.re, a.im, b.re, b.im}, xi[4] = {a.im, a.re, b.im, b.re};
+  return CDF{dot4(cr, xr, sr), dot4(cr, xi, si)};
+}
+static CDF split_c(std::complex<double> z) { CDF r; split(z.real(), r.re); split(z.imag(), r.im); return r; }
+static std::complex<double> merge_c(const CDF& v) { double a, b; merge(v.re.h, v.re.l, a); merge(v.im.h, v.im.l, b); return {a, b}; }
+int main() {
+  const int n = 10, N = 1 << n, G = 60;
+  std::mt19937_64 g(11);
+  std::normal_distribution<double> nd;
+  std::vector<LC> ex(N);
+  std::vector<std::complex<double>> f64(N);
+  std::vector<CDF> pairs(N);
+  long double nrm = 0;
+  for (int i = 0; i < N; ++i) { ex[i] = LC(nd(g), nd(g)); nrm += std::norm(ex[i]); }
+  for (int i = 0; i < N; ++i) { ex[i] /= std::sqrt(nrm); f64[i] = std::complex<double>((double)ex[i].real(), (double)ex[i].imag()); ex[i] = LC(f64[i].real(), f64[i].imag()); pairs[i] = split_c(f64[i]); }
+  for (int t = 0; t < G; ++t) {
+    // Haar-like U(2) from a random complex matrix (Gram-Schmidt), the qubit at random
+    std::complex<double> a(nd(g), nd(g)), b(nd(g), nd(g));
+    double s = std::sqrt(std::norm(a) + std::norm(b)); a /= s; b /= s;
+    std::complex<double> ph = std::polar(1.0, nd(g));
+    std::complex<double> m[4] = {a, -std::conj(b) * ph, b, std::conj(a) * ph};
+    int q = (int)(g() % n);
+    CDF md[4]; for (int k = 0; k < 4; ++k) md[k] = CDF{split_host(m[k].real()), split_host(m[k].imag())};
+    for (int i = 0; i < N; ++i) {
+      if (i & (1 << q)) continue;
+      int j = i | (1 << q);
+      LC x = ex[i], y = ex[j];
+      ex[i] = LC(m[0]) * x + LC(m[1]) * y; ex[j] = LC(m[2]) * x + LC(m[3]) * y;
+      // FP64 storage: split, row, round to FP64 every gate
+      CDF u = split_c(f64[i]), v = split_c(f64[j]);
+      f64[i] = merge_c(row(md[0], md[1], u, v)); f64[j] = merge_c(row(md[2], md[3], u, v));
+      // pair storage: rows on the pairs, no rounding in between
+      CDF pu = pairs[i], pv = pairs[j];
+      pairs[i] = row(md[0], md[1], pu, pv); pairs[j] = row(md[2], md[3], pu, pv);
+    }
+  }
+  double e64 = 0, epair = 0, diff = 0;
+  for (int i = 0; i < N; ++i) {
+    std::complex<double> p = merge_c(pairs[i]);
+    e64 = std::max(e64, (double)std::abs(LC(f64[i]) - ex[i]));
+    epair = std::max(epair, (double)std::abs(LC(p) - ex[i]));
+    diff = std::max(diff, std::abs(p - f64[i]));
+  }
+  printf("%.6e %.6e %.6e\n", e64, epair, diff);
+  return 0;
+}
+"""
+
+
+def test_pair_storage_chain_matches_fp64_storage(tmp_path):
+    """60 Haar-random gates on a normalised 10-qubit state in double-float arithmetic, once
+    rounding every amplitude to FP64 after each gate (FP64 storage) and once keeping the
+    double-float pairs until the end (pair storage), against long double: both stay at the
+    FP64 rounding level and agree with each other."""
+    src = tmp_path / "chain.cpp"
+    src.write_text(CHAIN)
+    exe = tmp_path / "chain"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", str(REPO / "intel-qs_gb300" / "csrc"),
+                    str(src), "-o", str(exe)], check=True)
+    e64, epair, diff = map(float, subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split())
+    assert e64 <= 1e-14 and epair <= 1e-14
+    assert diff <= 1e-14
