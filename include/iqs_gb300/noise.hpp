@@ -12,6 +12,7 @@
 // eigensystem and normalises it as the reference does.
 #pragma once
 
+#include <cmath>
 #include <complex>
 #include <cstdio>
 #include <initializer_list>
@@ -22,6 +23,7 @@
 #include <vector>
 
 #include "../iqsg.h"
+#include "tinymatrix.hpp"
 
 namespace iqs {
 
@@ -94,8 +96,8 @@ class RandomNumberGenerator {
 };
 
 template <class ValueType, unsigned M, unsigned align = alignof(ValueType)>
-class ChiMatrix {
-  static_assert(M != 0, "A zero-dimensional matrix is not allowed.");
+class ChiMatrix : public TinyMatrix<ValueType, M, M, align> {
+  using Base = TinyMatrix<ValueType, M, M, align>;
 
  public:
   using value_type = ValueType;
@@ -103,28 +105,24 @@ class ChiMatrix {
   using base_type = BaseType;
   using size_type = unsigned;
 
-  ChiMatrix() {
-    for (auto& r : data_)
-      for (auto& x : r) x = ValueType(0);
-  }
+  ChiMatrix() = default;
   template <class U>
-  ChiMatrix(std::initializer_list<std::initializer_list<U>> const& init) : ChiMatrix() {
-    unsigned i = 0;
-    for (auto& r : init) {
-      unsigned j = 0;
-      for (auto& x : r) data_[i][j++] = ValueType(x);
-      ++i;
-    }
+  ChiMatrix(U init[M][M]) : Base(init) {}
+  template <class U>
+  ChiMatrix(std::initializer_list<std::initializer_list<U>> const& init) : Base(init) {}
+  // From a chi matrix of another type or alignment, with its eigensystem.
+  template <class U, unsigned alignrhs>
+  ChiMatrix(ChiMatrix<U, M, alignrhs> const& rhs) : Base(static_cast<TinyMatrix<U, M, M, alignrhs> const&>(rhs)) {
+    for (auto const& x : rhs.GetEigenValues()) evalues_.push_back(value_type(x));
+    for (auto const& x : rhs.GetEigenProbabilities()) eprobs_.push_back(base_type(x));
+    for (auto const& x : rhs.GetEigenCumulativeProbabilities()) ecumprobs_.push_back(base_type(x));
+    for (auto const& v : rhs.GetEigenVectors()) evectors_.emplace_back(v.begin(), v.end());
   }
+  ChiMatrix(ChiMatrix const&) = default;
+  ChiMatrix& operator=(ChiMatrix const&) = default;
+  using Base::operator=;
 
-  ValueType& operator()(size_type i, size_type j) { return data_[i][j]; }
-  ValueType operator()(size_type i, size_type j) const { return data_[i][j]; }
-  ValueType* operator[](size_type i) { return data_[i]; }
-  const ValueType* operator[](size_type i) const { return data_[i]; }
-  size_type numRows() const { return M; }
-  size_type numCols() const { return M; }
-  size_type size() const { return M * M; }
-  ValueType* GetPtrToData() { return &data_[0][0]; }
+  ValueType* GetPtrToData() { return &this->data_[0][0]; }
 
   // Eigenvalues and standardised eigenvectors, chi = sum_k E_k |E_k><E_k|, then the
   // normalisation of src/chi_matrix.cpp:166-200. chi must be Hermitian.
@@ -132,8 +130,8 @@ class ChiMatrix {
     std::vector<double> chi(2 * M * M), ev(2 * M), vecs(2 * M * M), probs(M), cum(M);
     for (unsigned i = 0; i < M; ++i)
       for (unsigned j = 0; j < M; ++j) {
-        chi[2 * (i * M + j)] = data_[i][j].real();
-        chi[2 * (i * M + j) + 1] = data_[i][j].imag();
+        chi[2 * (i * M + j)] = this->data_[i][j].real();
+        chi[2 * (i * M + j) + 1] = this->data_[i][j].imag();
       }
     detail::rng_check(iqsg_chi_eigensystem(kPrec, M, chi.data(), ev.data(), vecs.data(), probs.data(), cum.data()));
     store(ev, vecs, probs, cum);
@@ -160,7 +158,7 @@ class ChiMatrix {
     for (unsigned i = 0; i < M; ++i)
       for (unsigned j = 0; j < M; ++j) {
         const bool block = (i == 1 || i == 3) && (j == 1 || j == 3);
-        if (data_[i][j] != (block ? value_type(0.5, 0) : value_type(0, 0)))
+        if (this->data_[i][j] != (block ? value_type(0.5, 0) : value_type(0, 0)))
           throw std::invalid_argument("EigensystemOfIdealHadamardChannel: chi is not the ideal Hadamard channel");
       }
     const value_type one(1, 0), zero(0, 0), e(1 / std::sqrt(2.0), 0);
@@ -187,7 +185,7 @@ class ChiMatrix {
   void Print(bool with_eigensystem = false) {
     std::cout << "chi_matrix :\n";
     for (unsigned i = 0; i < M; ++i) {
-      for (unsigned j = 0; j < M; ++j) std::cout << data_[i][j] << "\t";
+      for (unsigned j = 0; j < M; ++j) std::cout << this->data_[i][j] << "\t";
       std::cout << "\n";
     }
     if (!with_eigensystem) return;
@@ -235,7 +233,6 @@ class ChiMatrix {
         evectors_[k][i] = value_type((BaseType)vecs[2 * (k * M + i)], (BaseType)vecs[2 * (k * M + i) + 1]);
     }
   }
-  alignas(align) ValueType data_[M][M];
   std::vector<value_type> evalues_;
   std::vector<std::vector<value_type>> evectors_;
   std::vector<base_type> eprobs_;

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "../iqsg.h"
+#include "tinymatrix.hpp"
 #include "noise.hpp"
 
 using ComplexSP = std::complex<float>;
@@ -38,32 +39,6 @@ inline void check_status(int st) {
   if (st == IQSG_EINVAL) throw std::invalid_argument(iqsg_last_error());
   throw std::runtime_error(iqsg_last_error());
 }
-
-// Row-major fixed-size matrix (include/tinymatrix.hpp:39-306): m(i, j) and m[i][j].
-template <class ValueType, unsigned M, unsigned N = M, unsigned align = alignof(ValueType)>
-class TinyMatrix {
- public:
-  using value_type = ValueType;
-  TinyMatrix() { for (auto& r : data_) for (auto& x : r) x = ValueType(0); }
-  TinyMatrix(std::initializer_list<std::initializer_list<ValueType>> rows) : TinyMatrix() {
-    unsigned i = 0;
-    for (auto& r : rows) {
-      unsigned j = 0;
-      for (auto& x : r) data_[i][j++] = x;
-      ++i;
-    }
-  }
-  ValueType& operator()(unsigned i, unsigned j) { return data_[i][j]; }
-  ValueType operator()(unsigned i, unsigned j) const { return data_[i][j]; }
-  ValueType* operator[](unsigned i) { return data_[i]; }
-  const ValueType* operator[](unsigned i) const { return data_[i]; }
-  unsigned numRows() const { return M; }
-  unsigned numCols() const { return N; }
-  std::string name;
-
- private:
-  alignas(align) ValueType data_[M][N];
-};
 
 // Program qubit -> data position map (include/permutation.hpp:31-408).
 class Permutation {
@@ -148,10 +123,6 @@ template <class Type> struct extract_value_type;
 template <> struct extract_value_type<ComplexDP> { using value_type = double; };
 template <> struct extract_value_type<ComplexSP> { using value_type = float; };
 
-template <class Type>
-using TM2x2 = TinyMatrix<Type, 2, 2, 32>;
-template <class Type>
-using TM4x4 = TinyMatrix<Type, 4, 4, 32>;
 
 template <class Type = ComplexDP>
 class QubitRegister {
@@ -690,12 +661,6 @@ class QubitRegister {
 };
 
 }  // namespace iqs
-
-// The reference declares the matrix aliases at global scope (include/qureg.hpp:44-55).
-template <class Type>
-using TM2x2 = iqs::TinyMatrix<Type, 2, 2, 32>;
-template <class Type>
-using TM4x4 = iqs::TinyMatrix<Type, 4, 4, 32>;
 
 #include "noisy_qureg.hpp"
 #include "qubit_register_metric.hpp"

@@ -12,8 +12,8 @@
 
 using Reg = iqs::QubitRegister<ComplexDP>;
 
-static iqs::TM2x2<ComplexDP> read2(std::istringstream& in) {
-  iqs::TM2x2<ComplexDP> m;
+static TM2x2<ComplexDP> read2(std::istringstream& in) {
+  TM2x2<ComplexDP> m;
   for (int r = 0; r < 2; ++r)
     for (int c = 0; c < 2; ++c) { double a, b; in >> a >> b; m(r, c) = ComplexDP(a, b); }
   return m;
@@ -57,7 +57,7 @@ int main(int argc, char** argv) {
     else if (op == "CU1") { in >> a >> b; psi.ApplyControlled1QubitGate(a, b, read2(in)); }
     else if (op == "U2") {
       in >> a >> b;
-      iqs::TM4x4<ComplexDP> m;
+      TM4x4<ComplexDP> m;
       for (int r = 0; r < 4; ++r)
         for (int k = 0; k < 4; ++k) { double x, y; in >> x >> y; m(r, k) = ComplexDP(x, y); }
       psi.Apply2QubitGate(a, b, m);

@@ -22,3 +22,15 @@ def test_cpp_header_compiles(tmp_path):
                     str(REPO / "tests" / "cpp" / "qaoa_driver.cpp")], check=True)
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(REPO / "include"),
                     str(REPO / "tests" / "cpp" / "noise_driver.cpp")], check=True)
+
+
+def test_tinymatrix_and_chimatrix_reference_unit_tests(tmp_path):
+    """The reference's TinyMatrix / ChiMatrix unit tests against the drop-in header
+    (tests/cpp/tinymatrix_driver.cpp); host code only."""
+    exe = tmp_path / "tm"
+    libdir = REPO / "intel-qs_gb300" / "iqs_gb300"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-I", str(REPO / "include"),
+                    str(REPO / "tests" / "cpp" / "tinymatrix_driver.cpp"), "-L", str(libdir), "-liqsg",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
