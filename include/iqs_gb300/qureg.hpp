@@ -27,6 +27,7 @@
 
 #include "../iqsg.h"
 #include "tinymatrix.hpp"
+#include "permutation.hpp"
 #include "noise.hpp"
 
 using ComplexSP = std::complex<float>;
@@ -39,85 +40,6 @@ inline void check_status(int st) {
   if (st == IQSG_EINVAL) throw std::invalid_argument(iqsg_last_error());
   throw std::runtime_error(iqsg_last_error());
 }
-
-// Program qubit -> data position map (include/permutation.hpp:31-408).
-class Permutation {
- public:
-  std::vector<std::size_t> map, imap;
-  explicit Permutation(std::size_t n = 0) {
-    std::vector<std::size_t> m(n);
-    std::iota(m.begin(), m.end(), 0);
-    SetNewPermutationFromMap(m, "direct");
-  }
-  Permutation(const std::vector<std::size_t>& m, const std::string& style = "direct") { SetNewPermutationFromMap(m, style); }
-  unsigned operator[](std::size_t q) const { return (unsigned)map.at(q); }
-  std::size_t size() const { return map.size(); }
-  void SetNewPermutationFromMap(const std::vector<std::size_t>& m, const std::string& style = "direct") {
-    std::vector<char> seen(m.size(), 0);
-    for (auto p : m) {
-      if (p >= m.size() || seen[p]) throw std::invalid_argument("Permutation: not a permutation");
-      seen[p] = 1;
-    }
-    if (style == "direct") {
-      map = m;
-      imap.assign(m.size(), 0);
-      for (std::size_t q = 0; q < m.size(); ++q) imap[map[q]] = q;
-    } else if (style == "inverse") {
-      imap = m;
-      map.assign(m.size(), 0);
-      for (std::size_t p = 0; p < m.size(); ++p) map[imap[p]] = p;
-    } else {
-      throw std::invalid_argument("Permutation: style must be \"direct\" or \"inverse\"");
-    }
-  }
-  void ExchangeTwoElements(std::size_t e1, std::size_t e2) {
-    std::swap(map[e1], map[e2]);
-    imap[map[e1]] = e1;
-    imap[map[e2]] = e2;
-  }
-  std::size_t program2data_(std::size_t v) const {
-    std::size_t out = 0;
-    for (std::size_t p = 0; p < imap.size(); ++p) out |= ((v >> imap[p]) & 1u) << p;
-    return out;
-  }
-  std::size_t data2program_(std::size_t v) const {
-    std::size_t out = 0;
-    for (std::size_t q = 0; q < map.size(); ++q) out |= ((v >> map[q]) & 1u) << q;
-    return out;
-  }
-  // Program-order bit string of data index v: character q is bit map[q] (include/permutation.hpp:267-281).
-  std::string data2program(std::size_t v) const {
-    std::string s(map.size(), '0');
-    for (std::size_t q = 0; q < map.size(); ++q) s[q] = ((v >> map[q]) & 1u) ? '1' : '0';
-    return s;
-  }
-  std::string GetMapStr() const {
-    std::string s;
-    for (auto p : map) s += " " + std::to_string(p);
-    return s;
-  }
-};
-
-// Gate counts and greedy depth (include/gate_counter.hpp:18-95).
-class GateCounter {
- public:
-  explicit GateCounter(int n) : depth_(n, 0) {}
-  void OneQubitIncrement(int q) { ++total_; ++one_; ++depth_[q]; }
-  void TwoQubitIncrement(int a, int b) {
-    ++total_;
-    ++two_;
-    const int d = std::max(depth_[a], depth_[b]) + 1;
-    depth_[a] = depth_[b] = d;
-  }
-  int GetTotalGateCount() const { return total_; }
-  int GetOneQubitGateCount() const { return one_; }
-  int GetTwoQubitGateCount() const { return two_; }
-  int GetParallelDepth() const { return depth_.empty() ? 0 : *std::max_element(depth_.begin(), depth_.end()); }
-
- private:
-  int total_ = 0, one_ = 0, two_ = 0;
-  std::vector<int> depth_;
-};
 
 template <class Type> struct extract_value_type;
 template <> struct extract_value_type<ComplexDP> { using value_type = double; };
@@ -149,21 +71,32 @@ class QubitRegister {
   QubitRegister() : QubitRegister(1, "base", 0) {}
   QubitRegister(std::size_t num_qubits, std::string style = "", std::size_t base_index = 0,
                 std::size_t /*tmp_spacesize*/ = 0)
-      : n_((unsigned)num_qubits), perm_(num_qubits) {
+      : num_qubits(num_qubits), n_((unsigned)num_qubits), perm_(num_qubits) {
     check_status(iqsg_create(n_, kPrec, nullptr, &h_));
     Initialize(style, base_index);
   }
   // Imported state: the device memory at state is used in place and not freed.
   QubitRegister(std::size_t num_qubits, Type* device_state, std::size_t /*tmp_spacesize*/ = 0)
-      : n_((unsigned)num_qubits), perm_(num_qubits) {
+      : num_qubits(num_qubits), imported_state(true), n_((unsigned)num_qubits), perm_(num_qubits) {
     check_status(iqsg_create_from_device(n_, kPrec, device_state, nullptr, &h_));
   }
-  QubitRegister(const QubitRegister& in) : n_(in.n_), perm_(in.perm_), fusion_(false) {
+  QubitRegister(const QubitRegister& in) : num_qubits(in.num_qubits), n_(in.n_), perm_(in.perm_), fusion_(false) {
     const_cast<QubitRegister&>(in).ApplyFusedGates();
     check_status(iqsg_clone(in.h_, &h_));
   }
   QubitRegister& operator=(const QubitRegister&) = delete;
-  ~QubitRegister() { iqsg_destroy(h_); }
+  ~QubitRegister() {
+    delete gate_counter;
+    iqsg_destroy(h_);
+  }
+
+  // Public members of the reference's class (include/qureg.hpp:382-393) that callers and
+  // subclasses use: the size, the program-qubit map, the gate counter (null unless statistics
+  // are enabled) and whether the state memory belongs to the caller.
+  std::size_t num_qubits = 0;
+  Permutation* qubit_permutation = &perm_;
+  GateCounter* gate_counter = nullptr;
+  bool imported_state = false;
 
   // ---- information and access ----
   std::size_t NumQubits() const { return n_; }
@@ -253,9 +186,24 @@ class QubitRegister {
   }
 
   // ---- statistics ----
-  void EnableStatistics() { counter_.reset(new GateCounter((int)n_)); }
-  void DisableStatistics() { counter_.reset(); }
-  GateCounter* GetGateCounter() { return counter_.get(); }
+  void EnableStatistics() {
+    delete gate_counter;
+    gate_counter = new GateCounter((int)n_);
+  }
+  void DisableStatistics() {
+    delete gate_counter;
+    gate_counter = nullptr;
+  }
+  void ResetStatistics() {
+    DisableStatistics();
+    EnableStatistics();
+  }
+  // The gate counter's breakdown (the reference also prints its timer, which is not kept here).
+  void GetStatistics() {
+    if (!gate_counter) throw std::invalid_argument("GetStatistics: statistics are not enabled");
+    gate_counter->Breakdown();
+  }
+  GateCounter* GetGateCounter() { return gate_counter; }
 
   // ---- fusion ----
   void TurnOnFusion(unsigned log2llc = 20) { fusion_ = true; log2llc_ = log2llc; }
@@ -275,7 +223,7 @@ class QubitRegister {
   // ---- generic gates ----
   void Apply1QubitGate(unsigned qubit, const TM2x2<Type>& m) {
     const unsigned p = pos(qubit);
-    if (counter_) counter_->OneQubitIncrement((int)qubit);
+    if (gate_counter) gate_counter->OneQubitIncrement((int)qubit);
     iqsg_op op = make(IQSG_OP_1Q, p, 0, m8(m).data(), 8);
     if (fusion_) return queue(op);
     check_status(iqsg_apply_1q(h_, p, op.m));
@@ -283,7 +231,7 @@ class QubitRegister {
   void ApplyControlled1QubitGate(unsigned control, unsigned target, const TM2x2<Type>& m) {
     const unsigned pc = pos(control), pt = pos(target);
     if (control == target) throw std::invalid_argument("ApplyControlled1QubitGate: control == target");
-    if (counter_) counter_->TwoQubitIncrement((int)control, (int)target);
+    if (gate_counter) gate_counter->TwoQubitIncrement((int)control, (int)target);
     iqsg_op op = make(IQSG_OP_CTRL, pt, 0, m8(m).data(), 8);
     op.nctrl = 1;
     op.ctrl[0] = pc;
@@ -299,12 +247,12 @@ class QubitRegister {
     iqsg_op op = make(IQSG_OP_2Q, ph, pl, d, 32);
     if (fusion_) queue(op);
     else check_status(iqsg_apply_2q(h_, ph, pl, op.m));
-    if (counter_) counter_->TwoQubitIncrement((int)qubit_high, (int)qubit_low);
+    if (gate_counter) gate_counter->TwoQubitIncrement((int)qubit_high, (int)qubit_low);
   }
   void ApplyDiag(unsigned qubit_1, unsigned qubit_2, const TM4x4<Type>& m) {
     const unsigned p1 = pos(qubit_1), p2 = pos(qubit_2);
     if (qubit_1 == qubit_2) throw std::invalid_argument("ApplyDiag: qubits coincide");
-    if (counter_) counter_->TwoQubitIncrement((int)qubit_1, (int)qubit_2);
+    if (gate_counter) gate_counter->TwoQubitIncrement((int)qubit_1, (int)qubit_2);
     double d[8];
     for (int k = 0; k < 4; ++k) { d[2 * k] = (double)m(k, k).real(); d[2 * k + 1] = (double)m(k, k).imag(); }
     iqsg_op op = make(IQSG_OP_DIAG2, p1, p2, d, 8);
@@ -314,14 +262,15 @@ class QubitRegister {
 
   // The same diagonal as ApplyDiag, not counted as a gate (src/qureg_applydiag.cpp:17-51).
   void ApplyDiagSimp(unsigned qubit_1, unsigned qubit_2, const TM4x4<Type>& m) {
-    std::unique_ptr<GateCounter> keep(counter_.release());
+    GateCounter* keep = gate_counter;
+    gate_counter = nullptr;
     try {
       ApplyDiag(qubit_1, qubit_2, m);
     } catch (...) {
-      counter_.reset(keep.release());
+      gate_counter = keep;
       throw;
     }
-    counter_.reset(keep.release());
+    gate_counter = keep;
   }
 
   // ---- named one-qubit gates (src/qureg_apply1qubitgate.cpp:277-501) ----
@@ -415,12 +364,12 @@ class QubitRegister {
     if (c1 == c2 || c1 == t || c2 == t) throw std::invalid_argument("ApplyToffoli: qubits must differ");
     const unsigned pc[2] = {pos(c1), pos(c2)};
     const unsigned pt = pos(t);
-    if (counter_) {  // the reference's five two-qubit gates (src/qureg_applytoffoli.cpp:41-45)
-      counter_->TwoQubitIncrement((int)c1, (int)t);
-      counter_->TwoQubitIncrement((int)c2, (int)c1);
-      counter_->TwoQubitIncrement((int)c1, (int)t);
-      counter_->TwoQubitIncrement((int)c2, (int)c1);
-      counter_->TwoQubitIncrement((int)c2, (int)t);
+    if (gate_counter) {  // the reference's five two-qubit gates (src/qureg_applytoffoli.cpp:41-45)
+      gate_counter->TwoQubitIncrement((int)c1, (int)t);
+      gate_counter->TwoQubitIncrement((int)c2, (int)c1);
+      gate_counter->TwoQubitIncrement((int)c1, (int)t);
+      gate_counter->TwoQubitIncrement((int)c2, (int)c1);
+      gate_counter->TwoQubitIncrement((int)c2, (int)t);
     }
     const double x[8] = {0, 0, 1, 0, 1, 0, 0, 0};
     iqsg_op op = make(IQSG_OP_CTRL, pt, 0, x, 8);
@@ -465,11 +414,11 @@ class QubitRegister {
     ApplyFusedGates();
     std::vector<unsigned> p(qubits.size());
     for (std::size_t k = 0; k < qubits.size(); ++k) p[k] = pos(qubits[k]);
-    if (counter_)  // the reference's basis changes and their undo count as one-qubit gates
+    if (gate_counter)  // the reference's basis changes and their undo count as one-qubit gates
       for (std::size_t k = 0; k < qubits.size(); ++k)
         if (observables[k] == 1 || observables[k] == 2) {
-          counter_->OneQubitIncrement((int)qubits[k]);
-          counter_->OneQubitIncrement((int)qubits[k]);
+          gate_counter->OneQubitIncrement((int)qubits[k]);
+          gate_counter->OneQubitIncrement((int)qubits[k]);
         }
     double v = 0, n2 = 0;
     check_status(iqsg_expectation_pauli(h_, (unsigned)p.size(), p.data(), observables.data(), &v, &n2));
@@ -624,7 +573,7 @@ class QubitRegister {
     const unsigned p1 = pos(a), p2 = pos(b);
     if (a == b) throw std::invalid_argument("swap: qubits coincide");
     if (p1 > p2 && m(0, 1) != m(1, 0)) throw std::invalid_argument("swap: the 2x2 block must be symmetric");
-    if (counter_) counter_->TwoQubitIncrement((int)a, (int)b);
+    if (gate_counter) gate_counter->TwoQubitIncrement((int)a, (int)b);
     iqsg_op op = make(IQSG_OP_SWAPLIKE, p1, p2, m8(m).data(), 8);
     if (fusion_) return queue(op);
     check_status(iqsg_apply_swaplike(h_, p1, p2, op.m));
@@ -654,7 +603,6 @@ class QubitRegister {
   unsigned n_;
   iqsg_state* h_ = nullptr;
   Permutation perm_;
-  std::unique_ptr<GateCounter> counter_;
   bool fusion_ = false;
   unsigned log2llc_ = 20;
   std::vector<iqsg_op> fwindow_;

@@ -34,3 +34,15 @@ def test_tinymatrix_and_chimatrix_reference_unit_tests(tmp_path):
                     f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_permutation_and_gate_counter_reference_unit_tests(tmp_path):
+    """The reference's Permutation and GateCounter unit tests against the drop-in header
+    (tests/cpp/permutation_driver.cpp); host code only."""
+    exe = tmp_path / "pd"
+    libdir = REPO / "intel-qs_gb300" / "iqs_gb300"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-I", str(REPO / "include"),
+                    str(REPO / "tests" / "cpp" / "permutation_driver.cpp"), "-L", str(libdir), "-liqsg",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
