@@ -79,10 +79,52 @@ class Permutation:
         """Bits of v, least significant first (include/permutation.hpp:208-218)."""
         return "".join("1" if (v >> i) & 1 else "0" for i in range(num_bits))
 
-    def data2program(self, v: int) -> str:
-        """Program-order bit string of data index v: character q is bit map[q] of v
-        (include/permutation.hpp:267-281)."""
-        return "".join("1" if (v >> p) & 1 else "0" for p in self.map)
+    @staticmethod
+    def bin2dec(s: str) -> int:
+        """Inverse of dec2bin: character i is bit i (include/permutation.hpp:223-229)."""
+        return sum(1 << i for i, c in enumerate(s) if c == "1")
+
+    def data2program(self, v) -> str:
+        """Program-order bit string of a data index (or of a data bit string): character q is
+        bit map[q] (include/permutation.hpp:267-292)."""
+        s = v if isinstance(v, str) else self.dec2bin(int(v), len(self.map))
+        return "".join(s[p] for p in self.map)
+
+    def program2data(self, v) -> str:
+        """Data-order bit string of a program index (or program bit string): character p is
+        bit imap[p] (include/permutation.hpp:295-306)."""
+        s = v if isinstance(v, str) else self.dec2bin(int(v), len(self.map))
+        return "".join(s[q] for q in self.imap)
+
+    def Print(self) -> str:
+        line = f"qubit permutation: {self.GetMapStr()}"
+        print(line)
+        return line
+
+    def PrintRange(self) -> str:
+        lines = [f"map({i:3d}) = {self.bin2dec(self.data2program(i)):3d}" for i in range(1 << len(self.map))]
+        print("\n".join(lines))
+        return "\n".join(lines)
+
+    def ObtainIntemediateInverseMaps(self, target_map: List[int], M: int):
+        """For a reorder to target_map with positions [0, M) local, the inverse maps after the
+        local-only moves and after the global-only moves (include/permutation.hpp:345-380)."""
+        n = len(self.map)
+        if M > n or sorted(target_map) != list(range(n)):
+            raise ValueError("ObtainIntemediateInverseMaps: target_map must be a permutation and M <= n")
+        int_1 = list(self.imap)
+        for pos in range(M):
+            at = target_map[self.imap[pos]]
+            while at >= M:
+                at = target_map[self.imap[at]]
+            int_1[at] = self.imap[pos]
+        int_2 = list(int_1)
+        for pos in range(M, n):
+            at = target_map[int_1[pos]]
+            while at < M:
+                at = target_map[int_1[at]]
+            int_2[at] = int_1[pos]
+        return int_1, int_2
 
     def GetMapStr(self) -> str:
         return "".join(f" {p}" for p in self.map)
