@@ -27,6 +27,7 @@
 
 #include "../iqsg.h"
 #include "tinymatrix.hpp"
+#include "utils.hpp"
 #include "permutation.hpp"
 #include "noise.hpp"
 
@@ -390,7 +391,21 @@ class QubitRegister {
     check_status(iqsg_permute(h_, o.data(), m.data()));
     perm_ = np;
   }
+  // One GPU holds every qubit: local, global and pair-exchange reorders are the same reorder.
   void PermuteLocalQubits(std::vector<std::size_t> m, std::string s = "direct") { PermuteQubits(m, s); }
+  void PermuteGlobalQubits(std::vector<std::size_t> m, std::string s = "direct") { PermuteQubits(m, s); }
+  void PermuteByLocalGlobalExchangeOfQubitPairs(std::vector<std::size_t> m, std::string s = "direct") {
+    PermuteQubits(m, s);
+  }
+
+  // Bit manipulation helpers of the reference (include/qureg.hpp:168-181).
+  bool check_bit(std::size_t variable, std::size_t position) const { return (variable >> position) & 1u; }
+  std::size_t set_bit(std::size_t variable, std::size_t position) const {
+    return variable | (std::size_t(1) << position);
+  }
+  std::size_t clear_bit(std::size_t variable, std::size_t position) const {
+    return variable & ~(std::size_t(1) << position);
+  }
   void EmulateSwap(unsigned a, unsigned b) { pos(a); pos(b); perm_.ExchangeTwoElements(a, b); }
 
   // ---- measurement and expectation ----

@@ -104,6 +104,12 @@ int main() {
     g.Reset();
     CHECK(g.GetParallelDepth() == 0 && g.GetTotalGateCount() == 4);
   }
+  {  // conversion_test.hpp BasicUse and the bit utilities
+    CHECK(iqs::toString(1) == "1" && iqs::toString('a') == "a" && iqs::toString(std::string("s")) == "s");
+    CHECK(iqs::floor_power_of_two(5u) == 4 && iqs::floor_power_of_two(8u) == 8 && iqs::floor_power_of_two(1u) == 1);
+    CHECK(iqs::ilog2(std::size_t(1) << 33) == 33 && iqs::isPowerOf2(64) && !iqs::isPowerOf2(12) && !iqs::isPowerOf2(0));
+    CHECK(iqs::highestBit(0x90u) == 7 && iqs::popcnt(uint64_t(0xF0F0)) == 8 && UL(3) == std::size_t(3));
+  }
   std::printf("%d failures\n", failures);
   return failures ? 1 : 0;
 }
