@@ -17,6 +17,7 @@ from .rng import RandomNumberGenerator
 from .chi import CM4x4, CM16x16, ChiMatrix
 from .noisy import NoisyQureg, QubitRegisterMetric
 from .trotter import XXZChain
+from .environment import EnvFinalize, EnvFinalizeDummyRanks, EnvInit, MPIEnvironment
 from .qaoa import (GetExpectationValueFromCostFunction, GetExpectationValueSquaredFromCostFunction,
                    GetHistogramFromCostFunction, GetHistogramFromCostFunctionWithWeightsBinned,
                    GetHistogramFromCostFunctionWithWeightsRounded, ImplementQaoaLayerBasedOnCostFunction,
@@ -29,4 +30,5 @@ __all__ = [
     "InitializeVectorAsWeightedMaxCutCostFunction", "GetHistogramFromCostFunction",
     "GetHistogramFromCostFunctionWithWeightsRounded", "GetHistogramFromCostFunctionWithWeightsBinned",
     "QaoaMaxCut", "qaoa_energy", "BatchedAnsatz", "XXZChain", "RandomNumberGenerator", "ChiMatrix", "CM4x4", "CM16x16", "NoisyQureg", "QubitRegisterMetric",
+    "EnvInit", "EnvFinalize", "EnvFinalizeDummyRanks", "MPIEnvironment",
 ]
