@@ -182,7 +182,7 @@ class ChiMatrix : public TinyMatrix<ValueType, M, M, align> {
   std::vector<std::vector<value_type>> GetEigenVectors() const { return evectors_; }
 
   // src/chi_matrix.cpp:129-160.
-  void Print(bool with_eigensystem = false) {
+  void Print(bool with_eigensystem = true) {
     std::cout << "chi_matrix :\n";
     for (unsigned i = 0; i < M; ++i) {
       for (unsigned j = 0; j < M; ++j) std::cout << this->data_[i][j] << "\t";

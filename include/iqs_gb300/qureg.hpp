@@ -28,6 +28,7 @@
 #include "../iqsg.h"
 #include "tinymatrix.hpp"
 #include "utils.hpp"
+#include "mpi_env.hpp"
 #include "permutation.hpp"
 #include "noise.hpp"
 

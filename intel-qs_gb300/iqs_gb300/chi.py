@@ -173,7 +173,7 @@ class ChiMatrix:
         vf = np.ascontiguousarray(self._evecs, dtype=np.complex128).view(np.float64).reshape(-1)
         return ev, np.ascontiguousarray(self._cum, dtype=np.float64), vf
 
-    def Print(self, with_eigensystem: bool = False) -> str:
+    def Print(self, with_eigensystem: bool = True) -> str:
         """The reference's ChiMatrix::Print (src/chi_matrix.cpp:129-160), returned and printed."""
         out = ["chi_matrix :\n"]
         for i in range(self.M):

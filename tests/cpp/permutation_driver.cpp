@@ -110,6 +110,15 @@ int main() {
     CHECK(iqs::ilog2(std::size_t(1) << 33) == 33 && iqs::isPowerOf2(64) && !iqs::isPowerOf2(12) && !iqs::isPowerOf2(0));
     CHECK(iqs::highestBit(0x90u) == 7 && iqs::popcnt(uint64_t(0xF0F0)) == 8 && UL(3) == std::size_t(3));
   }
+  {  // the one-state pool environment
+    iqs::mpi::Environment::Init();
+    CHECK(iqs::mpi::Environment::GetSharedInstance() != nullptr && iqs::mpi::Environment::IsUsefulRank());
+    CHECK(iqs::mpi::Environment::GetStateSize() == 1 && iqs::mpi::Environment::GetNumStates() == 1);
+    CHECK(iqs::mpi::Environment::IncoherentSumOverAllStatesOfPool<double>(0.5) == 0.5);
+    iqs::mpi::StateBarrier();
+    iqs::mpi::Environment::Finalize();
+    CHECK(iqs::mpi::Environment::GetSharedInstance() == nullptr);
+  }
   std::printf("%d failures\n", failures);
   return failures ? 1 : 0;
 }
