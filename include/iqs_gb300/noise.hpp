@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <initializer_list>
 #include <iostream>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <type_traits>

@@ -19,6 +19,7 @@
 #include <cstring>
 #include <memory>
 #include <numeric>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -64,6 +65,35 @@ class QubitRegister {
     Type real_imag() const { return Type(*this); }
     BaseType real() const { return Type(*this).real(); }
     BaseType imag() const { return Type(*this).imag(); }
+    // Arithmetic as on the Type& the reference returns (std::complex's operators are templates
+    // and do not see the conversion): each read or write is one amplitude copy.
+    Amplitude& operator+=(const Type& v) { return *this = Type(*this) + v; }
+    Amplitude& operator-=(const Type& v) { return *this = Type(*this) - v; }
+    Amplitude& operator*=(const Type& v) { return *this = Type(*this) * v; }
+    Amplitude& operator/=(const Type& v) { return *this = Type(*this) / v; }
+    Amplitude& operator*=(BaseType v) { return *this = Type(*this) * v; }
+    Amplitude& operator/=(BaseType v) { return *this = Type(*this) / v; }
+    Type operator-() const { return -Type(*this); }
+    Type operator+() const { return Type(*this); }
+    friend Type operator+(const Amplitude& a, const Type& b) { return Type(a) + b; }
+    friend Type operator+(const Type& a, const Amplitude& b) { return a + Type(b); }
+    friend Type operator+(const Amplitude& a, const Amplitude& b) { return Type(a) + Type(b); }
+    friend Type operator-(const Amplitude& a, const Type& b) { return Type(a) - b; }
+    friend Type operator-(const Type& a, const Amplitude& b) { return a - Type(b); }
+    friend Type operator-(const Amplitude& a, const Amplitude& b) { return Type(a) - Type(b); }
+    friend Type operator*(const Amplitude& a, const Type& b) { return Type(a) * b; }
+    friend Type operator*(const Type& a, const Amplitude& b) { return a * Type(b); }
+    friend Type operator*(const Amplitude& a, const Amplitude& b) { return Type(a) * Type(b); }
+    friend Type operator*(const Amplitude& a, BaseType b) { return Type(a) * b; }
+    friend Type operator*(BaseType a, const Amplitude& b) { return a * Type(b); }
+    friend Type operator/(const Amplitude& a, const Type& b) { return Type(a) / b; }
+    friend Type operator/(const Amplitude& a, BaseType b) { return Type(a) / b; }
+    friend bool operator==(const Amplitude& a, const Type& b) { return Type(a) == b; }
+    friend bool operator!=(const Amplitude& a, const Type& b) { return Type(a) != b; }
+    friend std::ostream& operator<<(std::ostream& os, const Amplitude& a) { return os << Type(a); }
+    friend BaseType abs(const Amplitude& a) { return std::abs(Type(a)); }
+    friend BaseType norm(const Amplitude& a) { return std::norm(Type(a)); }
+    friend Type conj(const Amplitude& a) { return std::conj(Type(a)); }
 
    private:
     QubitRegister* r_;

@@ -10,8 +10,28 @@
 #include <stdexcept>
 #include <string>
 
+// Macros callers of the reference use (include/utils.hpp:6-20): compile-time notes, the
+// size_t cast, seconds, stringification.
+#ifndef DO_PRAGMA
+#define DO_PRAGMA(x) _Pragma(#x)
+#endif
+#ifndef TODO
+#define TODO(x) DO_PRAGMA(message("TODO - " #x))
+#endif
+#ifndef INFO
+#define INFO(x) DO_PRAGMA(message("INFO - " #x))
+#endif
 #ifndef UL
 #define UL(x) ((std::size_t)(x))
+#endif
+#ifndef sec
+#define sec() iqs::time_in_seconds()
+#endif
+#ifndef __str__
+#define __str__(s) #s
+#endif
+#ifndef xstr
+#define xstr(s) __str__(s)
 #endif
 
 namespace iqs {

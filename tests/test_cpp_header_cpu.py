@@ -1,6 +1,8 @@
 """The C++ drop-in header compiles on a machine without a GPU (syntax and templates only)."""
 import subprocess
 
+import pytest
+
 from conftest import REPO
 
 
@@ -46,3 +48,30 @@ def test_permutation_and_gate_counter_reference_unit_tests(tmp_path):
                     f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_reference_examples_compile_against_the_drop_in_header(tmp_path):
+    """Every example and tutorial program of the reference (examples/*.cpp, tutorials/*.cpp)
+    compiles unchanged against include/iqs_gb300/qureg.hpp: each source is copied next to an
+    include/qureg.hpp that includes the drop-in header, where its `#include "../include/qureg.hpp"`
+    finds it. Needs the reference's source tree (skipped without it)."""
+    import shutil
+
+    import oracle
+    srcs = sorted(list((oracle.REF_SRC / "examples").glob("*.cpp")) + list((oracle.REF_SRC / "tutorials").glob("*.cpp")))
+    if not srcs:
+        pytest.skip("the reference's source tree is not here")
+    (tmp_path / "include").mkdir()
+    (tmp_path / "include" / "qureg.hpp").write_text('#pragma once\n#include "iqs_gb300/qureg.hpp"\n')
+    work = tmp_path / "src"
+    work.mkdir()
+    failed = []
+    for src in srcs:
+        dst = work / src.name
+        shutil.copyfile(src, dst)
+        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(REPO / "include"), str(dst)],
+                           capture_output=True, text=True, cwd=str(work))
+        if r.returncode != 0:
+            failed.append((src.name, r.stderr[-400:]))
+    assert not failed, failed
+    assert len(srcs) >= 10
