@@ -22,6 +22,7 @@ class Environment {
 
   static void UpdateStateComm(int num_states) {
     if (num_states != 1) throw std::invalid_argument("UpdateStateComm: one process holds one state here");
+    std::printf("MPI not enabled.\n");
   }
   static bool IsUsefulRank() { return true; }
   static int GetPoolRank() { return 0; }

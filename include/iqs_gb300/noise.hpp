@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../iqsg.h"
+#include "mpi_env.hpp"
 #include "tinymatrix.hpp"
 
 namespace iqs {
@@ -61,7 +62,11 @@ class RandomNumberGenerator {
   RandomNumberGenerator& operator=(const RandomNumberGenerator&) = delete;
   ~RandomNumberGenerator() { iqsg_rng_destroy(r_); }
 
-  void SetSeedStreamPtrs(std::size_t seed) { detail::rng_check(iqsg_rng_set_seed(r_, seed)); }
+  void SetSeedStreamPtrs(std::size_t seed) {
+    detail::rng_check(iqsg_rng_set_seed_pool(r_, seed, (unsigned)mpi::Environment::GetNumStates(),
+                                             (unsigned)mpi::Environment::GetStateId(),
+                                             (unsigned)mpi::Environment::GetPoolRank()));
+  }
   std::size_t GetSeed() { return info(-1); }
   void SkipAhead(std::size_t num_skip, std::string shared = "local") {
     detail::rng_check(iqsg_rng_skip(r_, kPrec, num_skip, detail::stream_id(shared)));

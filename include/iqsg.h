@@ -128,8 +128,8 @@ int iqsg_init_uniform_random(iqsg_state* h, uint64_t seed, uint64_t skip, double
 
 /* Random number streams with the structure of the reference's RandomNumberGenerator
  * (include/rng_utils.hpp:46-130, src/rng_utils.cpp:13-225): three std::mt19937 streams,
- * 0 "pool" (seed), 1 "state" (seed + 1) and 2 "local" (seed + 2) -- one process being one state
- * of a one-state pool -- sharing one std::uniform_real_distribution and one
+ * 0 "pool" (seed), 1 "state" (seed + 1 + state id) and 2 "local" (seed + 1 + number of states +
+ * pool rank; see iqsg_rng_set_seed_pool) sharing one std::uniform_real_distribution and one
  * std::normal_distribution per base type, with per-stream counts: a uniform counts 1, a Gaussian
  * 2, a skip draws and discards uniforms. `precision` (IQSG_COMPLEX_SP / _DP) picks the base type
  * (float / double) as the reference's template argument does; values are returned as doubles. */
@@ -139,6 +139,11 @@ void iqsg_rng_destroy(iqsg_rng* r);
 /* Copy constructor (src/rng_utils.cpp:13-20): same seed, each stream's count skipped. */
 int iqsg_rng_clone(const iqsg_rng* src, int precision, iqsg_rng** out);
 int iqsg_rng_set_seed(iqsg_rng* r, uint64_t seed);                          /* SetSeedStreamPtrs */
+/* SetSeedStreamPtrs in a pool of num_states states: the state stream is seeded with
+ * seed + 1 + state_id and the local one with seed + 1 + num_states + pool_rank
+ * (src/rng_utils.cpp:84-99); iqsg_rng_set_seed is the one-state pool (1, 0, 0). */
+int iqsg_rng_set_seed_pool(iqsg_rng* r, uint64_t seed, unsigned num_states, unsigned state_id,
+                           unsigned pool_rank);
 int iqsg_rng_skip(iqsg_rng* r, int precision, uint64_t n, int stream);       /* SkipAhead */
 int iqsg_rng_uniform(iqsg_rng* r, int precision, double* out, uint64_t n, double a, double b,
                      int stream);                                            /* UniformRandomNumbers */

@@ -3,9 +3,9 @@
 // The gate itself runs through the ordinary gate kernels.
 //
 // Random numbers (include/rng_utils.hpp, src/rng_utils.cpp:13-225 of intel/intel-qs): three
-// std::mt19937 streams -- "pool" (seed), "state" (seed + 1) and "local" (seed + 2), for one
-// process being one state of a one-state pool -- sharing one std::uniform_real_distribution and
-// one std::normal_distribution per base type, with per-stream counts. A uniform draw counts 1,
+// std::mt19937 streams -- "pool" (seed), "state" (seed + 1 + state id) and "local" (seed + 1 +
+// number of states + pool rank) -- sharing one std::uniform_real_distribution and one
+// std::normal_distribution per base type, with per-stream counts. A uniform draw counts 1,
 // a Gaussian draw 2, a skip draws and discards uniforms. Values equal the reference's because the
 // same standard-library generator and distributions produce them; that is why this stays C++.
 //
@@ -22,6 +22,7 @@
 
 struct iqsg_rng {
   uint64_t seed = 0;
+  uint64_t stream_seed[3] = {0, 1, 2};  // seeds of the pool, state and local streams
   uint64_t count[3] = {0, 0, 0};
   std::mt19937 gen[3];
   std::uniform_real_distribution<double> ud{0.0, 1.0};
@@ -29,11 +30,16 @@ struct iqsg_rng {
   std::uniform_real_distribution<float> uf{0.0f, 1.0f};
   std::normal_distribution<float> nf{0.0f, 1.0f};
 
-  void set_seed(uint64_t s) {
+  // Pool stream: seed; state stream: seed + 1 + state id; local stream: seed + 1 + number of
+  // states + pool rank (src/rng_utils.cpp:84-99).
+  void set_seed(uint64_t s, uint64_t num_states = 1, uint64_t state_id = 0, uint64_t pool_rank = 0) {
     seed = s;
+    stream_seed[0] = s;
+    stream_seed[1] = s + 1 + state_id;
+    stream_seed[2] = s + 1 + num_states + pool_rank;
     for (int st = 0; st < 3; ++st) {
       count[st] = 0;
-      gen[st].seed((std::mt19937::result_type)(s + (uint64_t)st));
+      gen[st].seed((std::mt19937::result_type)stream_seed[st]);
     }
   }
   // Uniform numbers in [a, b) as a + (b - a) * u, u in [0, 1) (src/rng_utils.cpp:130-163).
@@ -275,6 +281,10 @@ extern "C" int iqsg_rng_clone(const iqsg_rng* src, int precision, iqsg_rng** out
   auto* r = new iqsg_rng();
   r->set_seed(src->seed);
   for (int s = 0; s < 3; ++s) {
+    r->stream_seed[s] = src->stream_seed[s];
+    r->gen[s].seed((std::mt19937::result_type)r->stream_seed[s]);
+  }
+  for (int s = 0; s < 3; ++s) {
     if (precision == IQSG_COMPLEX_DP)
       skip<double>(r, src->count[s], s);
     else
@@ -287,6 +297,15 @@ extern "C" int iqsg_rng_clone(const iqsg_rng* src, int precision, iqsg_rng** out
 extern "C" int iqsg_rng_set_seed(iqsg_rng* r, uint64_t seed) {
   if (!r) return fail(IQSG_EINVAL, "null random number generator");
   r->set_seed(seed);
+  return IQSG_OK;
+}
+
+extern "C" int iqsg_rng_set_seed_pool(iqsg_rng* r, uint64_t seed, unsigned num_states, unsigned state_id,
+                                      unsigned pool_rank) {
+  if (!r) return fail(IQSG_EINVAL, "null random number generator");
+  if (num_states == 0 || state_id >= num_states)
+    return fail(IQSG_EINVAL, "iqsg_rng_set_seed_pool: state %u of %u states", state_id, num_states);
+  r->set_seed(seed, num_states, state_id, pool_rank);
   return IQSG_OK;
 }
 
@@ -370,7 +389,7 @@ extern "C" int iqsg_init_random(iqsg_state* h, iqsg_rng* r, int stream) {
   int st = check_stream(stream, "iqsg_init_random");
   if (st) return st;
   if (r->seed == 0) return fail(IQSG_EINVAL, "iqsg_init_random: the generator needs a nonzero seed");
-  st = iqsg_init_uniform_random(h, r->seed + (uint64_t)stream, r->count[stream], -1.0, 1.0);
+  st = iqsg_init_uniform_random(h, r->stream_seed[stream], r->count[stream], -1.0, 1.0);
   if (st) return st;
   if (h->prec == IQSG_COMPLEX_DP)
     skip<double>(r, 2 * h->N, stream);

@@ -69,6 +69,7 @@ SIGNATURES = {
     "iqsg_rng_destroy": [_P],
     "iqsg_rng_clone": [_P, C.c_int, C.POINTER(_P)],
     "iqsg_rng_set_seed": [_P, _U64],
+    "iqsg_rng_set_seed_pool": [_P, _U64, C.c_uint, C.c_uint, C.c_uint],
     "iqsg_rng_skip": [_P, C.c_int, _U64, C.c_int],
     "iqsg_rng_uniform": [_P, C.c_int, _DP, _U64, _D, _D, C.c_int],
     "iqsg_rng_gaussian": [_P, C.c_int, _DP, _U64, C.c_int],

@@ -120,7 +120,7 @@ class MPIEnvironment:
         return float(t.item())
 
     @staticmethod
-    def UpdateStateComm(num_states: int) -> None:
+    def UpdateStateComm(num_states: int, do_print_info: bool = False) -> None:
         """Only the layout of one state per process exists; any other count is refused."""
         if int(num_states) != MPIEnvironment.GetSizeWorldComm():
             raise ValueError(f"UpdateStateComm: this engine keeps one state per process "

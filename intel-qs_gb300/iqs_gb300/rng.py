@@ -1,8 +1,9 @@
 """The reference's RandomNumberGenerator (include/rng_utils.hpp:46-130, src/rng_utils.cpp:13-225)
 over libiqsg's iqsg_rng: a seed and three std::mt19937 streams -- "pool" (seed), "state"
 (seed + 1 + state id) and "local" (seed + 1 + number of states + pool rank) -- each with a count
-of the numbers drawn or skipped. One process is one state of a one-state pool here, so the state
-id and pool rank are 0 and the number of states is 1.
+of the numbers drawn or skipped. Each process holds one state, so in a job of P processes
+(MPIEnvironment) there are P states and the state id is the pool rank; a single process is a
+one-state pool (state id and pool rank 0).
 
 The generator and its distributions live in the C++ library, so the numbers are those of the
 reference's standard-library classes. `precision` is the reference's template argument: "DP" for
@@ -54,7 +55,10 @@ class RandomNumberGenerator:
         return self._h
 
     def SetSeedStreamPtrs(self, seed: int) -> None:
-        check(lib.iqsg_rng_set_seed(self._h, int(seed)))
+        """Seed the three streams; in a pool of several one-state processes (MPIEnvironment) the
+        state and local streams differ by state id and pool rank as in the reference."""
+        from .environment import MPIEnvironment as E
+        check(lib.iqsg_rng_set_seed_pool(self._h, int(seed), E.GetNumStates(), E.GetStateId(), E.GetPoolRank()))
 
     def _info(self):
         seed = C.c_uint64()

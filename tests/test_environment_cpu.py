@@ -64,3 +64,44 @@ def test_two_ranks_are_two_states():
         assert p.exitcode == 0
     got = sorted(q.get(timeout=10) for _ in range(2))
     assert got == [(0, 0, 2, 1, 1, 3.0), (1, 1, 2, 1, 1, 3.0)]
+
+
+def _rng_rank(rank, world, port, q):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, str(REPO / "intel-qs_gb300"))
+    sys.path.insert(0, str(REPO))
+    import iqs_gb300 as iqs
+    import oracle
+    iqs.EnvInit()
+    try:
+        rng = iqs.RandomNumberGenerator()
+        rng.SetSeedStreamPtrs(777)
+        got = {s: list(rng.UniformRandomNumbers(5, 0, 1, s)) for s in ("pool", "state", "local")}
+        want = {"pool": 777, "state": 777 + 1 + rank, "local": 777 + 1 + world + rank}
+        ok = all(list(oracle.oracle_uniform_random(want[s], 0, 5, 0.0, 1.0, "DP")) == got[s] for s in got)
+        q.put((rank, ok, got["pool"][0]))
+    finally:
+        iqs.EnvFinalize()
+
+
+def test_stream_seeds_follow_the_pool():
+    """SetSeedStreamPtrs in a pool of two one-state ranks (src/rng_utils.cpp:84-99): the pool
+    stream is shared, the state and local streams are seeded by state id and pool rank."""
+    import torch.multiprocessing as mp
+    oracle_path = str(REPO)
+    if oracle_path not in sys.path:
+        sys.path.insert(0, oracle_path)
+    import oracle
+    oracle.build(ref=False)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rng_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=10) for _ in range(2))
+    assert [g[1] for g in got] == [True, True]
+    assert got[0][2] == got[1][2]  # the pool stream is common to the pool
