@@ -105,3 +105,15 @@ def test_stream_seeds_follow_the_pool():
     got = sorted(q.get(timeout=10) for _ in range(2))
     assert [g[1] for g in got] == [True, True]
     assert got[0][2] == got[1][2]  # the pool stream is common to the pool
+
+
+def test_intelqs_py_module_name():
+    """Programs that `import intelqs_py as iqs` find every name the reference's module binds
+    (pybind11/intelqs_py.cpp), apart from the MKL-only SetRndStreamPtrs."""
+    sys.path.insert(0, str(REPO / "intel-qs_gb300"))
+    import intelqs_py as iqs
+    for name in ("QubitRegister", "RandomNumberGenerator", "CM4x4", "CM16x16", "MPIEnvironment", "EnvInit",
+                 "EnvFinalize", "EnvFinalizeDummyRanks", "InitializeVectorAsMaxCutCostFunction",
+                 "ImplementQaoaLayerBasedOnCostFunction", "GetExpectationValueFromCostFunction",
+                 "GetHistogramFromCostFunctionWithWeightsBinned"):
+        assert hasattr(iqs, name), name
