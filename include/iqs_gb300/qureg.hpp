@@ -454,6 +454,14 @@ class QubitRegister {
     const BaseType p = GetProbability(q);
     return p < tol || std::abs(1 - p) < tol;
   }
+  // The value of a classical qubit (src/qureg_measure.cpp:184-260); a qubit that is not
+  // classical within the tolerance throws std::invalid_argument.
+  bool GetClassicalValue(unsigned q, BaseType tol = 1.e-13) {
+    const BaseType p = GetProbability(q);
+    if (p < tol) return false;
+    if (std::abs(1 - p) < tol) return true;
+    throw std::invalid_argument("GetClassicalValue: the qubit is not classical");
+  }
   BaseType ExpectationValue(std::vector<unsigned>& qubits, std::vector<unsigned>& observables, BaseType coeff = 1.) {
     if (qubits.size() != observables.size()) throw std::invalid_argument("ExpectationValue: size mismatch");
     if (qubits.empty()) return coeff;
