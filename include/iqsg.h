@@ -321,6 +321,25 @@ typedef enum {
                                   and writes FP64. Results differ by rounding only. */
 } iqsg_option;
 
+/* One fused sweep (one pass over the state) of a planned gate stream. */
+typedef struct {
+  unsigned k;          /* active positions of the sweep (0..4) */
+  unsigned pos[4];     /* those positions, slot order */
+  unsigned ops;        /* operations applied in the sweep */
+  unsigned one_qubit;  /* of which 2x2 gates (with or without controls) */
+  unsigned two_qubit;  /* dense, swap-type or excitation-preserving 4x4 gates */
+  unsigned diagonal;   /* phases and merged CZ runs (any positions, no slot needed) */
+} iqsg_sweep_info;
+
+/* The sweeps iqsg_apply_ops would run for `ops` on a register of num_qubits positions in the
+ * given precision and math (IQSG_MATH_*) with pass width `width` (0: the default) and default
+ * options otherwise -- the fusion plan of the reference's ApplyFusedGates
+ * (src/qureg_fusion.cpp:12-94), here one pass per sweep. Host only: allocates nothing, needs no
+ * GPU. *nsweeps gets the count; out (cap entries, may be null) one iqsg_sweep_info per sweep;
+ * *pair_storage whether the call would keep double-float pairs between the sweeps. */
+int iqsg_plan_ops(unsigned num_qubits, int precision, int math, unsigned width, const iqsg_op* ops,
+                  unsigned count, iqsg_sweep_info* out, unsigned cap, unsigned* nsweeps, int* pair_storage);
+
 /* Counters of a register: [0] double-float storage runs started by iqsg_apply_ops,
  * [1] kernels those runs launched (one range check and two kernels per sweep, one of which
  * returns at once). */

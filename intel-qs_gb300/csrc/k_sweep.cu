@@ -785,6 +785,65 @@ extern "C" int iqsg_apply_ops(iqsg_state* h, const iqsg_op* ops, unsigned count,
   return cuda_status(cudaGetLastError(), "iqsg_apply_ops");
 }
 
+// The sweeps iqsg_apply_ops would run for a gate stream on a register of num_qubits positions
+// with default options (no tile passes, no bulk pipeline, no native share), computed on the
+// host only: nothing is allocated or launched, no GPU is needed.
+extern "C" int iqsg_plan_ops(unsigned num_qubits, int precision, int math, unsigned width, const iqsg_op* ops,
+                             unsigned count, iqsg_sweep_info* out, unsigned cap, unsigned* nsweeps,
+                             int* pair_storage) {
+  if (count && !ops) return fail(IQSG_EINVAL, "iqsg_plan_ops: null op array");
+  if (num_qubits == 0 || num_qubits > 40) return fail(IQSG_EINVAL, "iqsg_plan_ops: %u qubits (1..40)", num_qubits);
+  if (precision != IQSG_COMPLEX_DP && precision != IQSG_COMPLEX_SP)
+    return fail(IQSG_EINVAL, "iqsg_plan_ops: unknown precision %d", precision);
+  if (math != IQSG_MATH_NATIVE && math != IQSG_MATH_EMULATED)
+    return fail(IQSG_EINVAL, "iqsg_plan_ops: unknown math %d", math);
+  if (width > (unsigned)kSweepMaxK) return fail(IQSG_EINVAL, "iqsg_plan_ops: width %u above %d", width, kSweepMaxK);
+  iqsg_state shape;  // sizes and options only: no memory behind it
+  shape.n = num_qubits;
+  shape.N = uint64_t(1) << num_qubits;
+  shape.prec = precision;
+  shape.math = math;
+  shape.sweep_width = width;
+  for (unsigned i = 0; i < count; ++i) {
+    const int st = check_op(&shape, ops[i], i);
+    if (st) return st;
+  }
+  CollectSweeps c;
+  {
+    SweepBuilder b(&c, std::max(1u, sweep_width(&shape)));
+    for (unsigned i = 0; i < count; ++i) queue_op(b, ops[i]);
+    b.flush();
+  }
+  if (nsweeps) *nsweeps = (unsigned)c.progs.size();
+  if (pair_storage) {  // the rule iqsg_apply_ops applies
+    bool pairs = precision == IQSG_COMPLEX_DP && math == IQSG_MATH_EMULATED && num_qubits >= 2 &&
+                 c.progs.size() >= kDfStoreMinSweeps;
+    for (unsigned i = 0; pairs && i < count; ++i) pairs = op_norm_bound(ops[i]) <= 1.0 + 1e-9;
+    for (const auto& P : c.progs) pairs = pairs && P.K <= 3;
+    *pair_storage = pairs ? 1 : 0;
+  }
+  if (out && cap < c.progs.size())
+    return fail(IQSG_EINVAL, "iqsg_plan_ops: %zu sweeps do not fit %u entries", c.progs.size(), cap);
+  for (size_t s = 0; out && s < c.progs.size(); ++s) {
+    const SweepParams& P = c.progs[s];
+    iqsg_sweep_info& o = out[s];
+    std::memset(&o, 0, sizeof o);
+    o.k = P.K;
+    for (unsigned j = 0; j < P.K; ++j) o.pos[j] = P.pos[j];
+    o.ops = P.nops;
+    for (unsigned k = 0; k < P.nops; ++k) {
+      switch (P.ops[k].kind) {
+        case SW_U2: ++o.one_qubit; break;
+        case SW_U4:
+        case SW_SWAPLIKE:
+        case SW_EXC: ++o.two_qubit; break;
+        default: ++o.diagonal; break;  // SW_PHASE, SW_CZSHIFT
+      }
+    }
+  }
+  return IQSG_OK;
+}
+
 extern "C" int iqsg_counters(const iqsg_state* h, uint64_t* counters) {
   if (!h || !counters) return fail(IQSG_EINVAL, "iqsg_counters: null argument");
   counters[0] = h->df_runs;

@@ -38,6 +38,12 @@ class Op(C.Structure):
 assert C.sizeof(Op) == 304, "iqsg_op layout mismatch"
 
 
+class SweepInfo(C.Structure):
+    """iqsg_sweep_info (include/iqsg.h): one fused sweep of a planned gate stream."""
+    _fields_ = [("k", C.c_uint), ("pos", C.c_uint * 4), ("ops", C.c_uint), ("one_qubit", C.c_uint),
+                ("two_qubit", C.c_uint), ("diagonal", C.c_uint)]
+
+
 class PauliTerm(C.Structure):
     """iqsg_pauli_term (include/iqsg.h)."""
     _fields_ = [("xmask", C.c_uint64), ("zmask", C.c_uint64), ("ny", C.c_int32), ("pad", C.c_int32),
@@ -65,6 +71,8 @@ SIGNATURES = {
     "iqsg_download": [_P, _P, _U64, _U64],
     "iqsg_init_uniform_random": [_P, _U64, _U64, _D, _D],
     "iqsg_counters": [_P, C.POINTER(_U64)],
+    "iqsg_plan_ops": [C.c_uint, C.c_int, C.c_int, C.c_uint, C.c_void_p, C.c_uint, C.POINTER(SweepInfo), C.c_uint,
+                      C.POINTER(C.c_uint), C.POINTER(C.c_int)],
     "iqsg_rng_create": [C.POINTER(_P)],
     "iqsg_rng_destroy": [_P],
     "iqsg_rng_clone": [_P, C.c_int, C.POINTER(_P)],

@@ -454,11 +454,19 @@ class QubitRegister:
 
     _flush = ApplyFusedGates
 
+    def PlanFusedGates(self) -> dict:
+        """The passes ApplyFusedGates would run for the queued gates, without running them
+        (see plan_ops)."""
+        return plan_ops(self._n, self._queue, precision=self.precision,
+                        math="emulated" if self._math == _lib.MATH_EMULATED else "native",
+                        width=getattr(self, "_width", 0))
+
     def SetSweepWidth(self, kmax: int) -> None:
         """Largest number of target qubits one fused pass holds in registers (1..4, 0 =
         default for the precision)."""
         self._flush()
         check(lib.iqsg_set_sweep_width(self._h, int(kmax)))
+        self._width = int(kmax)
 
     def SetNativeShare(self, sixteenths: int) -> None:
         """Emulated ComplexDP fused sweeps: let sixteenths/16 of the warps use native FP64 (the
@@ -903,3 +911,21 @@ for _name in ("SetMath", "RawState", "synchronize", "Initialize", "Initializatio
               "AmplitudeWiseSum", "__eq__"):
     setattr(QubitRegister, _name, _flushing(getattr(QubitRegister, _name)))
 QubitRegister.PermuteLocalQubits = QubitRegister.PermuteQubits
+
+
+def plan_ops(num_qubits: int, ops, *, precision: str = "DP", math: str = "native", width: int = 0) -> dict:
+    """The fused sweeps iqsg_apply_ops would run for a list of `_lib.Op` gates on a register of
+    num_qubits positions (host only; no GPU needed): {"sweeps": [{"k", "positions", "ops",
+    "one_qubit", "two_qubit", "diagonal"}, ...], "pair_storage": bool}."""
+    arr = (_lib.Op * max(1, len(ops)))(*ops)
+    n = C.c_uint()
+    pairs = C.c_int()
+    check(lib.iqsg_plan_ops(int(num_qubits), _PREC[precision], _MATH[math], int(width), C.cast(arr, C.c_void_p),
+                            len(ops), None, 0, C.byref(n), C.byref(pairs)))
+    info = (_lib.SweepInfo * max(1, n.value))()
+    check(lib.iqsg_plan_ops(int(num_qubits), _PREC[precision], _MATH[math], int(width), C.cast(arr, C.c_void_p),
+                            len(ops), info, n.value, C.byref(n), C.byref(pairs)))
+    sweeps = [{"k": s.k, "positions": list(s.pos)[:s.k], "ops": s.ops, "one_qubit": s.one_qubit,
+               "two_qubit": s.two_qubit, "diagonal": s.diagonal} for s in info[:n.value]]
+    return {"sweeps": sweeps, "pair_storage": bool(pairs.value)}
+
